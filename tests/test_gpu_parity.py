@@ -1,0 +1,177 @@
+"""GPU parity: the CUDA library (through its C ABI) against the CPU oracle.
+
+Tolerances: every FP64 operator (product, transfers, inverse diagonals,
+preconditioner) agrees with the oracle to <= 1e-11 relative (different
+summation order only); integer data (numbering, fixed sets, level sizes) is
+bit-exact; a full FP64 solve takes the oracle's iteration count (+-1) and its
+displacement agrees to <= 1e-5 relative L2 with a true relative residual
+< 1e-6 (the bar of the reference's CPU path, rtol 1e-6).
+"""
+import numpy as np
+import pytest
+
+import oracle
+from vulkanfem_gb300 import api, domains
+
+pytestmark = pytest.mark.gpu
+
+OP_TOL = 1e-11
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def _random_domain(shape, fill, seed):
+    rng = np.random.default_rng(seed)
+    vox = (rng.random(shape) < fill).astype(np.uint8)
+    vox[0] = 1
+    vox = domains.keep_grounded(vox)
+    ids = domains.node_numbering(vox)
+    fixed = np.sort(ids[0][ids[0] >= 0])
+    top = np.sort(ids[-1][ids[-1] >= 0])
+    lv = np.zeros((top.size, 3))
+    lv[:, 2] = -1.0 / max(top.size, 1)
+    return vox, fixed, top, lv
+
+
+CASES = {
+    "cantilever": lambda: (lambda d: (d.voxels, d.fixed, d.load_nodes, d.load_values, 3, 0))(domains.cantilever()),
+    "odd_7x5x3": lambda: _random_domain((3, 5, 7), 0.8, 5)[:4] + (2, 0),
+    "porous_20": lambda: _random_domain((20, 20, 20), 0.7, 1)[:4] + (3, 0),
+    "skip_16": lambda: _random_domain((16, 16, 16), 0.75, 2)[:4] + (3, 1),
+}
+
+
+@pytest.fixture(scope="module", params=sorted(CASES))
+def case(request):
+    vox, fixed, ln, lv, levels, skip = CASES[request.param]()
+    ke = domains.hex8_stiffness()
+    o = oracle.Oracle(vox, ke, fixed, levels, skip)
+    A = api.assembleSystemMatrix(vox, ke, fixed, levels, skip)
+    f = np.zeros(o.num_dofs())
+    f.reshape(-1, 3)[ln] = lv
+    return {"name": request.param, "o": o, "A": A, "f": f, "vox": vox, "fixed": fixed}
+
+
+def test_hierarchy_integer_parity(case):
+    o, A = case["o"], case["A"]
+    assert A.num_levels == o.num_levels
+    assert A.coarse_free_dofs == o.num_coarse_free()
+    for lv in range(o.num_levels):
+        assert A.num_dofs(lv) == o.num_dofs(lv)
+        assert np.array_equal(A.fixed_nodes(lv), o.fixed(lv))
+
+
+def test_inverse_diagonal_parity(case):
+    o, A = case["o"], case["A"]
+    for lv in range(o.num_levels):
+        assert rel(A.inverse_diagonal(lv), o.inv_diag(lv)) < OP_TOL
+
+
+def test_operator_parity(case):
+    o, A = case["o"], case["A"]
+    x = np.random.default_rng(0).standard_normal(o.num_dofs())
+    assert rel(A @ x, o.matvec(x)) < OP_TOL
+
+
+def test_transfer_parity(case):
+    o, A = case["o"], case["A"]
+    rng = np.random.default_rng(1)
+    for lv in range(o.num_levels - 1):
+        v = rng.standard_normal(o.num_dofs(lv))
+        assert rel(A.restrict(lv, v), o.restrict(lv, v)) < OP_TOL
+        c = rng.standard_normal(o.num_dofs(lv + 1))
+        assert rel(A.interpolate(lv, c), o.interpolate(lv, c)) < OP_TOL
+
+
+def test_preconditioner_parity(case):
+    o, A = case["o"], case["A"]
+    r = np.random.default_rng(2).standard_normal(o.num_dofs())
+    M = api.MultigridPreconditioner(A)
+    assert rel(M.solve(r), o.precond(r)) < 1e-10
+
+
+def test_fp64_solve_parity(case):
+    o, A, f = case["o"], case["A"], case["f"]
+    x_o, it_o, _ = o.pcg(f, tol=1e-6)
+    u, st = api.solveWithKompute(A, f)
+    assert abs(st["iterations"] - it_o) <= 1
+    assert st["rel_residual"] < 1e-6
+    assert rel(u, x_o) < 1e-5
+
+
+def test_mixed_precision_solve(case):
+    o, A, f = case["o"], case["A"], case["f"]
+    x_tight, _, _ = o.pcg(f, tol=1e-10)
+    u, st = A.solve(f, precision="mixed")
+    assert st["rel_residual"] < 1e-6
+    r = f - o.matvec(u)
+    assert np.linalg.norm(r) / np.linalg.norm(f) < 1e-6
+    assert rel(u, x_tight) < 1e-4
+
+
+def test_vcycle_mode_solve(case):
+    o, A, f = case["o"], case["A"], case["f"]
+    x_tight, _, _ = o.pcg(f, tol=1e-10)
+    u, st = A.solve(f, mg_mode="vcycle")
+    assert st["rel_residual"] < 1e-6
+    assert rel(u, x_tight) < 1e-4
+    u2, st2 = A.solve(f, mg_mode="vcycle", precision="mixed", flexible=True)
+    assert st2["rel_residual"] < 1e-6
+
+
+def test_warm_start_and_repeat(case):
+    o, A, f = case["o"], case["A"], case["f"]
+    u, st = A.solve(f)
+    u2, st2 = A.solve(f, u0=u)
+    assert st2["iterations"] <= 1
+    u3, st3 = A.solve(f)
+    assert np.array_equal(u, u3) and st3["iterations"] == st["iterations"]
+
+
+def test_armadillo_parity(armadillo):
+    """The reference's own fixture, with Ke0.dat used verbatim in its index order."""
+    o = oracle.Oracle(armadillo["voxels"], armadillo["ke0"], armadillo["fixed"], 3, 0)
+    o.set_threads(8)
+    A = api.assembleSystemMatrix(armadillo["voxels"], armadillo["ke0"], armadillo["fixed"], 3, 0)
+    assert A.num_dofs(0) == 562455
+    for lv in range(3):
+        assert np.array_equal(A.fixed_nodes(lv), o.fixed(lv))
+        assert rel(A.inverse_diagonal(lv), o.inv_diag(lv)) < OP_TOL
+    x = np.random.default_rng(3).standard_normal(A.rows())
+    assert rel(A @ x, o.matvec(x)) < OP_TOL
+    f = o.load_vector(armadillo["load_nodes"], armadillo["load_values"])
+    A.set_loads(armadillo["load_nodes"], armadillo["load_values"])
+    u, st = A.solve()
+    x_o, it_o, _ = o.pcg(f)
+    assert abs(st["iterations"] - it_o) <= 1
+    assert st["rel_residual"] < 1e-6
+    assert rel(u, x_o) < 1e-5
+    assert f @ u == pytest.approx(f @ x_o, rel=1e-6)
+
+
+def test_per_voxel_modulus():
+    """Extension with no reference counterpart: Ke_e = E_e Ke.  Uniform E = c scales
+    the solution by 1/c; a random field keeps the operator symmetric and matches a
+    dense element-by-element product."""
+    from tests import structured_ref as sr
+    vox, fixed, ln, lv = _random_domain((10, 12, 9), 0.75, 9)
+    ke = domains.hex8_stiffness()
+    A1 = api.assembleSystemMatrix(vox, ke, fixed, 3)
+    A2 = api.assembleSystemMatrix(vox, ke, fixed, 3, E=np.full(vox.shape, 2.5, np.float32))
+    f = np.zeros(A1.rows())
+    f.reshape(-1, 3)[ln] = lv
+    u1, _ = A1.solve(f, rtol=1e-10)
+    u2, _ = A2.solve(f, rtol=1e-10)
+    assert rel(2.5 * u2, u1) < 1e-8
+    E = np.random.default_rng(4).lognormal(0, 0.5, vox.shape).astype(np.float32)
+    A3 = api.assembleSystemMatrix(vox, ke, fixed, 3, E=E)
+    mask = sr.used_mask(vox.astype(bool))
+    fm = np.zeros(mask.shape, bool)
+    fm.reshape(-1)[np.flatnonzero(mask.reshape(-1))[fixed]] = True
+    x = np.random.default_rng(5).standard_normal(A3.rows())
+    y_ref = sr.to_compressed(sr.matvec(vox * E.astype(np.float64), ke, sr.to_dense(x, mask), fm), mask)
+    assert rel(A3 @ x, y_ref) < 1e-12
+    u3, st3 = A3.solve(f, mg_mode="vcycle")
+    assert st3["rel_residual"] < 1e-6

@@ -1,0 +1,845 @@
+// api.cu -- problem lifecycle, the device-resident PCG driver and the C ABI.
+//
+// Replaces solveWithKompute (src/FEMGPU.cpp:32-554 of the reference) and the
+// Eigen CG driver solveWithEigen (src/FEM.cpp:589-637).  The reference's GPU
+// loop uploads and downloads full vectors and solves the coarsest level on the
+// host every iteration (FEMGPU.cpp:471-541); here every step of an iteration
+// is a kernel on one stream, the coarsest solve is a dense inverse applied on
+// the device, and chunks of iterations are replayed as one CUDA graph with the
+// host polling a device-side `done` flag between chunks.  The iteration count
+// and stopping rule are Eigen 3.4's (x0 = 0, stop when |r|^2 < tol^2 |b|^2 on the
+// recursive residual, iterations counted without the breaking pass).
+#include <cuda_runtime.h>
+#include <cusolverDn.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "kernels.h"
+
+using namespace vfem;
+
+namespace {
+
+std::atomic<long long> g_launches{0};
+thread_local std::string g_lastError;
+
+constexpr int64_t kMaxCoarseFree = 32768;
+
+struct DevLevel {
+    Grid g;
+    int div = 2;
+    double scale = 1.0;
+    int64_t nused = 0, nelem = 0;
+    float* E = nullptr;
+    uint8_t* flags = nullptr;
+    int32_t* nodeStore = nullptr;
+    double* dinv64 = nullptr;
+    float* dinv32 = nullptr;
+    double* dinvR64 = nullptr;
+    float* dinvR32 = nullptr;
+    double *r64 = nullptr, *z64 = nullptr, *t64 = nullptr;
+    float *r32 = nullptr, *z32 = nullptr, *t32 = nullptr;
+    int64_t nvec() const { return 3 * g.nnode; }
+};
+
+struct GraphKey {
+    int mg, prec, flexible, pre, post, replace, chunk;
+    double omega;
+    bool operator<(const GraphKey& o) const {
+        return std::tie(mg, prec, flexible, pre, post, replace, chunk, omega) <
+               std::tie(o.mg, o.prec, o.flexible, o.pre, o.post, o.replace, o.chunk, o.omega);
+    }
+};
+
+struct CachedGraph {
+    cudaGraphExec_t exec = nullptr;
+    long long kernels = 0;
+};
+
+}  // namespace
+
+struct vfem_problem {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    KeData ke;
+    Hierarchy H;
+    std::vector<DevLevel> L;
+    // level-0 solver vectors (dense storage)
+    double *f64 = nullptr, *x64 = nullptr, *p64 = nullptr, *Ap64 = nullptr;
+    float *p32 = nullptr, *Ap32 = nullptr;
+    // coarsest dense inverse
+    int64_t nc = 0;
+    int32_t* freeDof = nullptr;
+    double* Kinv64 = nullptr;
+    float* Kinv32 = nullptr;
+    double* cb64 = nullptr;
+    float* cb32 = nullptr;
+    // reductions / scalars
+    Scalars* S = nullptr;
+    Scalars* hS = nullptr;
+    RedBuf rb{};
+    // compressed staging
+    double* dComp = nullptr;  // 3 * nused(level 0) (largest level)
+    double* hIn = nullptr;    // pinned
+    double* hOut = nullptr;   // pinned
+    // constants for the kernels
+    double op64[45 + 576];
+    float op32[45 + 576];
+    std::map<GraphKey, CachedGraph> graphs;
+    bool rhsSet = false;
+    long long launches = 0;
+};
+
+namespace {
+
+vfem_status fail(vfem_status s, const std::string& msg) {
+    g_lastError = msg;
+    return s;
+}
+
+#define CK(call)                                                                                   \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess) {                                                                   \
+            return fail(e_ == cudaErrorMemoryAllocation ? VFEM_ERR_OUT_OF_MEMORY : VFEM_ERR_CUDA,  \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                       \
+        }                                                                                          \
+    } while (0)
+
+template <typename T>
+cudaError_t dalloc(T** p, int64_t n) {
+    cudaError_t e = cudaMalloc((void**)p, (size_t)std::max<int64_t>(n, 1) * sizeof(T));
+    if (e != cudaSuccess) return e;
+    return cudaMemset(*p, 0, (size_t)std::max<int64_t>(n, 1) * sizeof(T));
+}
+
+template <typename T>
+cudaError_t upload(T** p, const std::vector<T>& v) {
+    cudaError_t e = dalloc(p, (int64_t)v.size());
+    if (e != cudaSuccess || v.empty()) return e;
+    return cudaMemcpy(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+}
+
+void freeProblem(vfem_problem* p) {
+    if (!p) return;
+    cudaSetDevice(p->device);
+    for (auto& kv : p->graphs)
+        if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+    for (auto& l : p->L) {
+        cudaFree(l.E); cudaFree(l.flags); cudaFree(l.nodeStore);
+        cudaFree(l.dinv64); cudaFree(l.dinv32); cudaFree(l.dinvR64); cudaFree(l.dinvR32);
+        cudaFree(l.r64); cudaFree(l.z64); cudaFree(l.t64); cudaFree(l.r32); cudaFree(l.z32); cudaFree(l.t32);
+    }
+    cudaFree(p->f64); cudaFree(p->x64); cudaFree(p->p64); cudaFree(p->Ap64); cudaFree(p->p32); cudaFree(p->Ap32);
+    cudaFree(p->freeDof); cudaFree(p->Kinv64); cudaFree(p->Kinv32); cudaFree(p->cb64); cudaFree(p->cb32);
+    cudaFree(p->S); cudaFree(p->rb.partials); cudaFree(p->rb.ticket); cudaFree(p->dComp);
+    if (p->hS) cudaFreeHost(p->hS);
+    if (p->hIn) cudaFreeHost(p->hIn);
+    if (p->hOut) cudaFreeHost(p->hOut);
+    if (p->stream) cudaStreamDestroy(p->stream);
+    delete p;
+}
+
+LaunchCtx ctx(vfem_problem* p) { return LaunchCtx{p->stream, p->S, p->rb}; }
+
+vfem_status buildCoarse(vfem_problem* p) {
+    const HostLevel& hc = p->H.L.back();
+    DevLevel& dc = p->L.back();
+    int64_t n = (int64_t)p->H.coarseFreeDof.size();
+    p->nc = n;
+    if (n > kMaxCoarseFree)
+        return fail(VFEM_ERR_COARSE_TOO_LARGE, "coarsest level has " + std::to_string(n) +
+                                                   " free DOFs; add levels (limit " +
+                                                   std::to_string(kMaxCoarseFree) + ")");
+    if (n == 0) return VFEM_OK;
+    CK(upload(&p->freeDof, p->H.coarseFreeDof));
+    int32_t* dFreeNode = nullptr;
+    CK(upload(&dFreeNode, p->H.coarseFreeNode));
+    CK(dalloc(&p->Kinv64, n * n));
+    CK(dalloc(&p->Kinv32, n * n));
+    CK(dalloc(&p->cb64, n));
+    CK(dalloc(&p->cb32, n));
+    // Kc = 2^(L-1+skip) sum_e E_e Ke on the free DOFs (assembleK, FEM.cpp:19-63,498-513).
+    p->launches += launchAssembleCoarse(p->stream, dc.g, dc.E, dFreeNode, p->ke.Ke, hc.scale, p->Kinv64, n);
+    CK(cudaGetLastError());
+    cusolverDnHandle_t h = nullptr;
+    if (cusolverDnCreate(&h) != CUSOLVER_STATUS_SUCCESS) {
+        cudaFree(dFreeNode);
+        return fail(VFEM_ERR_CUDA, "cusolverDnCreate failed");
+    }
+    cusolverDnSetStream(h, p->stream);
+    int lw1 = 0, lw2 = 0;
+    vfem_status st = VFEM_OK;
+    double* work = nullptr;
+    int* info = nullptr;
+    int hinfo = 0;
+    if (cusolverDnDpotrf_bufferSize(h, CUBLAS_FILL_MODE_LOWER, (int)n, p->Kinv64, (int)n, &lw1) !=
+            CUSOLVER_STATUS_SUCCESS ||
+        cusolverDnDpotri_bufferSize(h, CUBLAS_FILL_MODE_LOWER, (int)n, p->Kinv64, (int)n, &lw2) !=
+            CUSOLVER_STATUS_SUCCESS) {
+        st = fail(VFEM_ERR_CUDA, "cusolver buffer size query failed");
+    }
+    if (st == VFEM_OK && (cudaMalloc(&work, sizeof(double) * (size_t)std::max(1, std::max(lw1, lw2))) != cudaSuccess ||
+                          cudaMalloc(&info, sizeof(int)) != cudaSuccess))
+        st = fail(VFEM_ERR_OUT_OF_MEMORY, "cusolver workspace");
+    if (st == VFEM_OK) {
+        if (cusolverDnDpotrf(h, CUBLAS_FILL_MODE_LOWER, (int)n, p->Kinv64, (int)n, work, std::max(lw1, lw2), info) !=
+            CUSOLVER_STATUS_SUCCESS)
+            st = fail(VFEM_ERR_CUDA, "cusolverDnDpotrf failed");
+        else {
+            cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, p->stream);
+            cudaStreamSynchronize(p->stream);
+            if (hinfo != 0) st = fail(VFEM_ERR_SINGULAR, "coarsest system is not positive definite (potrf info " +
+                                                            std::to_string(hinfo) + ")");
+        }
+    }
+    if (st == VFEM_OK) {
+        if (cusolverDnDpotri(h, CUBLAS_FILL_MODE_LOWER, (int)n, p->Kinv64, (int)n, work, std::max(lw1, lw2), info) !=
+            CUSOLVER_STATUS_SUCCESS)
+            st = fail(VFEM_ERR_CUDA, "cusolverDnDpotri failed");
+        else {
+            cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, p->stream);
+            cudaStreamSynchronize(p->stream);
+            if (hinfo != 0) st = fail(VFEM_ERR_SINGULAR, "coarsest inverse failed (potri info " +
+                                                            std::to_string(hinfo) + ")");
+        }
+    }
+    if (st == VFEM_OK) {
+        p->launches += launchSymmetrizeLowerToFull(p->stream, p->Kinv64, n);
+        p->launches += launchConvert<double, float>(p->stream, n * n, p->Kinv64, p->Kinv32);
+        if (cudaStreamSynchronize(p->stream) != cudaSuccess) st = fail(VFEM_ERR_CUDA, "coarse inverse kernels");
+    }
+    cudaFree(work);
+    cudaFree(info);
+    cudaFree(dFreeNode);
+    cusolverDnDestroy(h);
+    return st;
+}
+
+vfem_status createImpl(const uint8_t* vox, int nx, int ny, int nz, const double* Ke, const float* E,
+                       const int64_t* fixed, int64_t nfixed, int numLevels, int skip, vfem_problem** out) {
+    if (!vox || !Ke || !out || (nfixed > 0 && !fixed))
+        return fail(VFEM_ERR_INVALID_ARGUMENT, "null pointer argument");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(VFEM_ERR_NO_DEVICE, "no CUDA device");
+    vfem_problem* p = new vfem_problem();
+    CK(cudaGetDevice(&p->device));
+    vfem_status st = prepareKe(Ke, p->ke);
+    if (st != VFEM_OK) {
+        delete p;
+        return fail(st, "Ke has non-finite entries");
+    }
+    std::string err;
+    st = buildHierarchy(vox, nx, ny, nz, E, fixed, nfixed, numLevels, skip, p->ke, p->H, err);
+    if (st != VFEM_OK) {
+        delete p;
+        return fail(st, err);
+    }
+    for (int i = 0; i < 45; ++i) {
+        p->op64[i] = p->ke.ks[i];
+        p->op32[i] = (float)p->ke.ks[i];
+    }
+    for (int i = 0; i < 576; ++i) {
+        p->op64[45 + i] = p->ke.Ke[i];
+        p->op32[45 + i] = (float)p->ke.Ke[i];
+    }
+    auto bail = [&](vfem_status s) {
+        freeProblem(p);
+        return s;
+    };
+#define CKP(call)                                                                                         \
+    do {                                                                                                  \
+        cudaError_t e_ = (call);                                                                          \
+        if (e_ != cudaSuccess)                                                                            \
+            return bail(fail(e_ == cudaErrorMemoryAllocation ? VFEM_ERR_OUT_OF_MEMORY : VFEM_ERR_CUDA,     \
+                             std::string(#call) + ": " + cudaGetErrorString(e_)));                        \
+    } while (0)
+    CKP(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking));
+    CKP(setKernelAttributes());
+    p->L.resize(p->H.L.size());
+    for (size_t i = 0; i < p->H.L.size(); ++i) {
+        const HostLevel& h = p->H.L[i];
+        DevLevel& d = p->L[i];
+        d.g = h.g;
+        d.div = h.divider;
+        d.scale = h.scale;
+        d.nused = (int64_t)h.nodeStore.size();
+        d.nelem = h.nelem;
+        CKP(upload(&d.E, h.E));
+        CKP(upload(&d.flags, h.flags));
+        CKP(upload(&d.nodeStore, h.nodeStore));
+        CKP(upload(&d.dinv64, h.dinv));
+        CKP(upload(&d.dinvR64, h.dinvRedisc));
+        int64_t nv = d.nvec();
+        CKP(dalloc(&d.dinv32, nv));
+        CKP(dalloc(&d.dinvR32, nv));
+        launchConvert<double, float>(p->stream, nv, d.dinv64, d.dinv32);
+        launchConvert<double, float>(p->stream, nv, d.dinvR64, d.dinvR32);
+        p->launches += 2;
+        CKP(dalloc(&d.r64, nv)); CKP(dalloc(&d.z64, nv)); CKP(dalloc(&d.t64, nv));
+        CKP(dalloc(&d.r32, nv)); CKP(dalloc(&d.z32, nv)); CKP(dalloc(&d.t32, nv));
+    }
+    int64_t nv0 = p->L[0].nvec();
+    CKP(dalloc(&p->f64, nv0)); CKP(dalloc(&p->x64, nv0)); CKP(dalloc(&p->p64, nv0)); CKP(dalloc(&p->Ap64, nv0));
+    CKP(dalloc(&p->p32, nv0)); CKP(dalloc(&p->Ap32, nv0));
+    CKP(dalloc(&p->S, 1));
+    CKP(dalloc(&p->rb.partials, 2 * (int64_t)kMaxRedBlocks));
+    CKP(dalloc(&p->rb.ticket, 1));
+    CKP(dalloc(&p->dComp, 3 * p->L[0].nused));
+    CKP(cudaMallocHost((void**)&p->hS, sizeof(Scalars)));
+    CKP(cudaMallocHost((void**)&p->hIn, sizeof(double) * 3 * (size_t)std::max<int64_t>(1, p->L[0].nused)));
+    CKP(cudaMallocHost((void**)&p->hOut, sizeof(double) * 3 * (size_t)std::max<int64_t>(1, p->L[0].nused)));
+    st = buildCoarse(p);
+    if (st != VFEM_OK) return bail(st);
+    CKP(cudaStreamSynchronize(p->stream));
+    CKP(cudaGetLastError());
+    g_launches += p->launches;
+    *out = p;
+    return VFEM_OK;
+#undef CKP
+}
+
+// ------------------------------------------------------------------ solver pieces
+// Every helper returns the number of kernels it enqueued.
+
+template <typename T>
+T* lvR(DevLevel& l);
+template <>
+double* lvR<double>(DevLevel& l) { return l.r64; }
+template <>
+float* lvR<float>(DevLevel& l) { return l.r32; }
+template <typename T>
+T* lvZ(DevLevel& l);
+template <>
+double* lvZ<double>(DevLevel& l) { return l.z64; }
+template <>
+float* lvZ<float>(DevLevel& l) { return l.z32; }
+template <typename T>
+T* lvT(DevLevel& l);
+template <>
+double* lvT<double>(DevLevel& l) { return l.t64; }
+template <>
+float* lvT<float>(DevLevel& l) { return l.t32; }
+template <typename T>
+T* lvDinv(DevLevel& l, bool redisc);
+template <>
+double* lvDinv<double>(DevLevel& l, bool redisc) { return redisc ? l.dinvR64 : l.dinv64; }
+template <>
+float* lvDinv<float>(DevLevel& l, bool redisc) { return redisc ? l.dinvR32 : l.dinv32; }
+template <typename T>
+const void* opc(vfem_problem* p);
+template <>
+const void* opc<double>(vfem_problem* p) { return p->op64; }
+template <>
+const void* opc<float>(vfem_problem* p) { return p->op32; }
+template <typename T>
+T* kinv(vfem_problem* p);
+template <>
+double* kinv<double>(vfem_problem* p) { return p->Kinv64; }
+template <>
+float* kinv<float>(vfem_problem* p) { return p->Kinv32; }
+template <typename T>
+T* cbuf(vfem_problem* p);
+template <>
+double* cbuf<double>(vfem_problem* p) { return p->cb64; }
+template <>
+float* cbuf<float>(vfem_problem* p) { return p->cb32; }
+
+template <typename T>
+MatvecArgs<T> mvArgs(vfem_problem* p, int lv, const T* x, T* y, int mode) {
+    DevLevel& l = p->L[lv];
+    MatvecArgs<T> a{};
+    a.g = l.g;
+    a.E = l.E;
+    a.flags = l.flags;
+    a.x = x;
+    a.y = y;
+    a.scale = l.scale;
+    a.mode = mode;
+    a.checkDone = 1;
+    return a;
+}
+
+template <typename T>
+int matvec(vfem_problem* p, const MatvecArgs<T>& a) {
+    return launchMatvec<T>(ctx(p), a, p->ke.structured, opc<T>(p));
+}
+
+// z = M^-1 r on level `lv` (r, z given); returns kernels; on level 0 the final
+// pass produces r.z (and z.aux) with epilogue `epi`.  *outZ receives the buffer
+// holding the result (it differs from z in the multiplicative cycle when the
+// number of post-sweeps is odd).
+template <typename T>
+int vcycle(vfem_problem* p, const vfem_options& o, int lv, T* r, T* z, T** outZ, const T* aux, int epi) {
+    const int L = (int)p->L.size();
+    int n = 0;
+    DevLevel& l = p->L[lv];
+    LaunchCtx c = ctx(p);
+    if (lv == L - 1) {
+        // Coarsest: exact dense-inverse solve on the free DOFs; fixed and unused DOFs stay 0.
+        n += launchCoarseSolve<T>(c, kinv<T>(p), p->nc, p->freeDof, r, cbuf<T>(p), z, 1);
+        if (lv == 0 && epi != EPI_NONE) n += launchDots<T>(c, l.nvec(), r, z, aux ? z : nullptr, aux, epi, 1);
+        *outZ = z;
+        return n;
+    }
+    DevLevel& lc = p->L[lv + 1];
+    if (o.mg_mode == VFEM_MG_REFERENCE) {
+        // Additive cycle of the reference (MultigridPreconditioner.hpp:158-193).
+        n += launchRestrict<T>(c, l.g, lc.g, lc.div, r, lvR<T>(lc), 1);
+        T* zc = nullptr;
+        n += vcycle<T>(p, o, lv + 1, lvR<T>(lc), lvZ<T>(lc), &zc, nullptr, EPI_NONE);
+        n += launchProlongSmooth<T>(c, l.g, lc.g, lc.div, zc, r, lvDinv<T>(l, false), l.flags, z, 2.0, lv == 0 ? 1 : 0,
+                                    lv == 0 ? aux : nullptr, lv == 0 ? epi : EPI_NONE, 1);
+        *outZ = z;
+        return n;
+    }
+    // Multiplicative V-cycle with damped Jacobi on the rediscretised level operators.
+    const T* dinv = lvDinv<T>(l, true);
+    T* cur = z;
+    T* other = lvT<T>(l);
+    n += launchJacobiZero<T>(c, l.g, r, dinv, l.flags, cur, o.omega, 1);
+    for (int s = 1; s < o.pre_sweeps; ++s) {
+        MatvecArgs<T> a = mvArgs<T>(p, lv, cur, other, MV_SMOOTH);
+        a.f = r;
+        a.dinv = dinv;
+        a.omega = o.omega;
+        n += matvec<T>(p, a);
+        std::swap(cur, other);
+    }
+    {
+        MatvecArgs<T> a = mvArgs<T>(p, lv, cur, other, MV_RESID0);
+        a.f = r;
+        n += matvec<T>(p, a);
+    }
+    n += launchRestrict<T>(c, l.g, lc.g, lc.div, other, lvR<T>(lc), 1);
+    T* zc = nullptr;
+    n += vcycle<T>(p, o, lv + 1, lvR<T>(lc), lvZ<T>(lc), &zc, nullptr, EPI_NONE);
+    n += launchProlongAdd<T>(c, l.g, lc.g, lc.div, zc, l.flags, cur, 1);
+    for (int s = 0; s < o.post_sweeps; ++s) {
+        MatvecArgs<T> a = mvArgs<T>(p, lv, cur, other, MV_SMOOTH);
+        a.f = r;
+        a.dinv = dinv;
+        a.omega = o.omega;
+        if (lv == 0 && s == o.post_sweeps - 1 && epi != EPI_NONE) {
+            a.dot0 = DOT_F_OUT;
+            a.dot1 = aux ? 1 : 0;
+            a.aux = aux;
+            a.epi = epi;
+        }
+        n += matvec<T>(p, a);
+        std::swap(cur, other);
+    }
+    if (lv == 0 && o.post_sweeps == 0 && epi != EPI_NONE)
+        n += launchDots<T>(c, l.nvec(), r, cur, aux ? cur : nullptr, aux, epi, 1);
+    *outZ = cur;
+    return n;
+}
+
+// Preconditioner application on level 0 (identity when mg_mode == NONE).
+template <typename T>
+int precondition(vfem_problem* p, const vfem_options& o, T* r, T* z, T** outZ, const T* aux, int epi) {
+    if (o.mg_mode == VFEM_MG_NONE) {
+        DevLevel& l = p->L[0];
+        int n = launchConvert<T, T>(p->stream, l.nvec(), r, z);
+        n += launchDots<T>(ctx(p), l.nvec(), r, z, aux ? z : nullptr, aux, epi, 1);
+        *outZ = z;
+        return n;
+    }
+    return vcycle<T>(p, o, 0, r, z, outZ, aux, epi);
+}
+
+// One PCG iteration (after initialisation).  FP64: Eigen's loop body.
+// Mixed: FP32 vectors, FP64 x, conditional FP64 true-residual pass.
+int iteration(vfem_problem* p, const vfem_options& o, double** zOut64, float** zOut32) {
+    DevLevel& l0 = p->L[0];
+    const int64_t n = l0.nvec();
+    LaunchCtx c = ctx(p);
+    int k = 0;
+    if (o.precision == VFEM_PREC_FP64) {
+        MatvecArgs<double> a = mvArgs<double>(p, 0, p->p64, p->Ap64, MV_AX);
+        a.dot0 = DOT_X_OUT;
+        a.epi = EPI_ALPHA;
+        k += matvec<double>(p, a);
+        k += launchUpdateXR<double, double>(c, n, p->x64, l0.r64, p->p64, p->Ap64);
+        double* z = nullptr;
+        k += precondition<double>(p, o, l0.r64, l0.z64, &z, o.flexible ? p->Ap64 : nullptr, EPI_BETA);
+        k += launchUpdateP<double>(c, n, p->p64, z, 0);
+        *zOut64 = z;
+    } else {
+        MatvecArgs<float> a = mvArgs<float>(p, 0, p->p32, p->Ap32, MV_AX);
+        a.dot0 = DOT_X_OUT;
+        a.epi = EPI_ALPHA;
+        k += matvec<float>(p, a);
+        k += launchUpdateXR<double, float>(c, n, p->x64, l0.r32, p->p32, p->Ap32);
+        MatvecArgs<double> t = mvArgs<double>(p, 0, p->x64, l0.r64, MV_RESID);
+        t.f = p->f64;
+        t.y32 = l0.r32;
+        t.dot0 = DOT_OUT_OUT;
+        t.epi = EPI_TRUE;
+        t.condTrue = 1;
+        k += matvec<double>(p, t);
+        float* z = nullptr;
+        k += precondition<float>(p, o, l0.r32, l0.z32, &z, o.flexible ? p->Ap32 : nullptr, EPI_BETA);
+        k += launchUpdateP<float>(c, n, p->p32, z, 0);
+        *zOut32 = z;
+    }
+    return k;
+}
+
+vfem_status checkOptions(const vfem_options& o) {
+    if (!(o.rtol > 0) || o.mg_mode < 0 || o.mg_mode > 2 || o.precision < 0 || o.precision > 1 ||
+        (o.mg_mode == VFEM_MG_VCYCLE && (!(o.omega > 0) || o.pre_sweeps < 1 || o.post_sweeps < 0)) ||
+        o.check_every < 1 || o.check_every > 1024 || o.replace_every < 0)
+        return fail(VFEM_ERR_INVALID_ARGUMENT, "invalid solver options");
+    return VFEM_OK;
+}
+
+vfem_status solveImpl(vfem_problem* p, const vfem_options* optIn, bool haveX0, vfem_stats* st) {
+    vfem_options o;
+    vfem_options_default(&o);
+    if (optIn) o = *optIn;
+    vfem_status s = checkOptions(o);
+    if (s != VFEM_OK) return s;
+    CK(cudaSetDevice(p->device));
+    DevLevel& l0 = p->L[0];
+    const int64_t n = l0.nvec();
+    const long long maxIter = o.max_iter > 0 ? o.max_iter : 2 * 3 * l0.nused;
+    const bool mixed = o.precision == VFEM_PREC_MIXED;
+    LaunchCtx c = ctx(p);
+    long long launches = 0;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    CK(cudaEventRecord(e0, p->stream));
+    launches += launchInitScalars(p->stream, p->S, o.rtol, maxIter, o.flexible, mixed ? 1 : 0,
+                                  mixed ? o.replace_every : 0);
+    // ---- initial residual, norms, first direction
+    double* z64 = nullptr;
+    float* z32 = nullptr;
+    if (haveX0) {
+        MatvecArgs<double> a = mvArgs<double>(p, 0, p->x64, l0.r64, MV_RESID);
+        a.f = p->f64;
+        a.checkDone = 0;
+        if (mixed) a.y32 = l0.r32;
+        launches += matvec<double>(p, a);
+    } else {
+        launches += launchFill<double>(p->stream, n, p->x64, 0.0);
+        launches += launchConvert<double, double>(p->stream, n, p->f64, l0.r64);
+        if (mixed) launches += launchConvert<double, float>(p->stream, n, p->f64, l0.r32);
+    }
+    launches += launchDots<double>(c, n, p->f64, p->f64, l0.r64, l0.r64, EPI_INIT, 0);
+    if (mixed) {
+        launches += precondition<float>(p, o, l0.r32, l0.z32, &z32, nullptr, EPI_RHO0);
+        launches += launchUpdateP<float>(c, n, p->p32, z32, 1);
+    } else {
+        launches += precondition<double>(p, o, l0.r64, l0.z64, &z64, nullptr, EPI_RHO0);
+        launches += launchUpdateP<double>(c, n, p->p64, z64, 1);
+    }
+    CK(cudaGetLastError());
+    // ---- chunked iterations replayed from a cached graph
+    GraphKey key{o.mg_mode, o.precision, o.flexible, o.pre_sweeps, o.post_sweeps, mixed ? o.replace_every : 0,
+                 o.check_every, o.omega};
+    CachedGraph& cg = p->graphs[key];
+    if (!cg.exec) {
+        cudaGraph_t graph = nullptr;
+        CK(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
+        long long k = 0;
+        for (int i = 0; i < o.check_every; ++i) k += iteration(p, o, &z64, &z32);
+        cudaError_t ec = cudaStreamEndCapture(p->stream, &graph);
+        if (ec != cudaSuccess) return fail(VFEM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ec));
+        ec = cudaGraphInstantiate(&cg.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ec != cudaSuccess) {
+            cg.exec = nullptr;
+            return fail(VFEM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ec));
+        }
+        cg.kernels = k;
+    }
+    long long chunks = 0;
+    const long long maxChunks = maxIter / o.check_every + 2;
+    for (;;) {
+        CK(cudaMemcpyAsync(p->hS, p->S, sizeof(Scalars), cudaMemcpyDeviceToHost, p->stream));
+        CK(cudaStreamSynchronize(p->stream));
+        if (p->hS->done != RUNNING || chunks >= maxChunks) break;
+        CK(cudaGraphLaunch(cg.exec, p->stream));
+        launches += cg.kernels;
+        ++chunks;
+    }
+    CK(cudaEventRecord(e1, p->stream));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    Scalars hs = *p->hS;
+    // ---- true residual at exit (outside the timed solve for FP64)
+    double relTrue = NAN;
+    if (mixed && hs.done == CONVERGED && hs.replacements > 0 && hs.rhsNorm2 > 0) {
+        relTrue = std::sqrt(hs.rrTrue / hs.rhsNorm2);
+    } else if (o.compute_true_residual && hs.rhsNorm2 > 0) {
+        MatvecArgs<double> a = mvArgs<double>(p, 0, p->x64, l0.t64, MV_RESID);
+        a.f = p->f64;
+        a.checkDone = 0;
+        a.dot0 = DOT_OUT_OUT;
+        a.epi = EPI_STORE;
+        launches += matvec<double>(p, a);
+        CK(cudaMemcpyAsync(p->hS, p->S, sizeof(Scalars), cudaMemcpyDeviceToHost, p->stream));
+        CK(cudaStreamSynchronize(p->stream));
+        relTrue = std::sqrt(p->hS->red0 / hs.rhsNorm2);
+    } else if (hs.rhsNorm2 == 0) {
+        relTrue = 0.0;
+    }
+    CK(cudaGetLastError());
+    p->launches += launches;
+    g_launches += launches;
+    vfem_status result = VFEM_OK;
+    if (hs.done == BREAKDOWN) result = VFEM_ERR_BREAKDOWN;
+    else if (hs.done == MAXITER || hs.done == RUNNING) result = VFEM_ERR_NOT_CONVERGED;
+    if (st) {
+        st->iterations = hs.iter;
+        st->matvecs = hs.matvecs;
+        st->residual_replacements = hs.replacements;
+        st->rel_residual = relTrue;
+        st->recursive_rel_residual = hs.rhsNorm2 > 0 ? std::sqrt(hs.rr / hs.rhsNorm2) : 0.0;
+        st->solve_ms = ms;
+        st->kernel_launches = launches;
+        st->status = result;
+    }
+    if (result == VFEM_ERR_BREAKDOWN) g_lastError = "PCG breakdown (p^T A p <= 0 or non-finite scalar)";
+    if (result == VFEM_ERR_NOT_CONVERGED) g_lastError = "maximum iterations reached";
+    return result;
+}
+
+vfem_status toDenseHost(vfem_problem* p, int lv, const double* host, double* dense, double* h2dMs) {
+    DevLevel& l = p->L[lv];
+    std::memcpy(p->hIn, host, sizeof(double) * 3 * (size_t)l.nused);
+    CK(cudaMemcpyAsync(p->dComp, p->hIn, sizeof(double) * 3 * (size_t)l.nused, cudaMemcpyHostToDevice, p->stream));
+    CK(cudaMemsetAsync(dense, 0, sizeof(double) * (size_t)l.nvec(), p->stream));
+    p->launches += launchScatterCompressed<double>(p->stream, l.nused, l.nodeStore, p->dComp, dense);
+    g_launches += 1;
+    (void)h2dMs;
+    return VFEM_OK;
+}
+
+vfem_status fromDenseHost(vfem_problem* p, int lv, const double* dense, double* host) {
+    DevLevel& l = p->L[lv];
+    p->launches += launchGatherCompressed<double>(p->stream, l.nused, l.nodeStore, dense, p->dComp);
+    g_launches += 1;
+    CK(cudaMemcpyAsync(p->hOut, p->dComp, sizeof(double) * 3 * (size_t)l.nused, cudaMemcpyDeviceToHost, p->stream));
+    CK(cudaStreamSynchronize(p->stream));
+    std::memcpy(host, p->hOut, sizeof(double) * 3 * (size_t)l.nused);
+    return VFEM_OK;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ C ABI
+extern "C" {
+
+void vfem_options_default(vfem_options* o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->rtol = 1e-6;
+    o->max_iter = 0;
+    o->mg_mode = VFEM_MG_REFERENCE;
+    o->precision = VFEM_PREC_FP64;
+    o->omega = 0.6;
+    o->pre_sweeps = 1;
+    o->post_sweeps = 1;
+    o->replace_every = 50;
+    o->flexible = 0;
+    o->check_every = 8;
+    o->compute_true_residual = 1;
+}
+
+const char* vfem_status_string(vfem_status s) {
+    switch (s) {
+        case VFEM_OK: return "ok";
+        case VFEM_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case VFEM_ERR_CUDA: return "CUDA error";
+        case VFEM_ERR_OUT_OF_MEMORY: return "out of device memory";
+        case VFEM_ERR_NOT_CONVERGED: return "not converged";
+        case VFEM_ERR_BREAKDOWN: return "PCG breakdown";
+        case VFEM_ERR_SINGULAR: return "coarsest system singular";
+        case VFEM_ERR_EMPTY: return "empty domain";
+        case VFEM_ERR_COARSE_TOO_LARGE: return "coarsest level too large";
+        case VFEM_ERR_NO_DEVICE: return "no CUDA device";
+        case VFEM_ERR_TIMEOUT: return "timeout";
+    }
+    return "unknown status";
+}
+
+const char* vfem_last_error_message(void) { return g_lastError.c_str(); }
+
+int64_t vfem_kernel_launch_count(void) { return g_launches.load(); }
+
+vfem_status vfem_hex8_stiffness(double E, double nu, double* Ke) {
+    if (!Ke || !(E > 0) || !(nu > -1.0 && nu < 0.5)) return fail(VFEM_ERR_INVALID_ARGUMENT, "bad E or nu");
+    hex8Stiffness(E, nu, Ke);
+    return VFEM_OK;
+}
+
+vfem_status vfem_problem_create(const uint8_t* voxels, int32_t nx, int32_t ny, int32_t nz, const double* Ke,
+                                const float* E_or_null, const int64_t* fixed_nodes, int64_t nfixed,
+                                int32_t num_levels, int32_t skip_levels, vfem_problem** out) {
+    if (out) *out = nullptr;
+    return createImpl(voxels, nx, ny, nz, Ke, E_or_null, fixed_nodes, nfixed, num_levels, skip_levels, out);
+}
+
+void vfem_problem_destroy(vfem_problem* p) { freeProblem(p); }
+
+vfem_status vfem_problem_info(const vfem_problem* p, int32_t level, int64_t* num_nodes, int64_t* num_elements,
+                              int32_t* num_levels, int64_t* coarse_free_dofs) {
+    if (!p) return fail(VFEM_ERR_INVALID_ARGUMENT, "null problem");
+    if (level < 0 || level >= (int)p->L.size()) return fail(VFEM_ERR_INVALID_ARGUMENT, "level out of range");
+    if (num_nodes) *num_nodes = p->L[level].nused;
+    if (num_elements) *num_elements = p->L[level].nelem;
+    if (num_levels) *num_levels = (int32_t)p->L.size();
+    if (coarse_free_dofs) *coarse_free_dofs = p->nc;
+    return VFEM_OK;
+}
+
+vfem_status vfem_problem_set_rhs(vfem_problem* p, const double* f) {
+    if (!p || !f) return fail(VFEM_ERR_INVALID_ARGUMENT, "null argument");
+    CK(cudaSetDevice(p->device));
+    for (int64_t i = 0; i < 3 * p->L[0].nused; ++i)
+        if (!std::isfinite(f[i])) return fail(VFEM_ERR_INVALID_ARGUMENT, "non-finite right-hand side");
+    vfem_status s = toDenseHost(p, 0, f, p->f64, nullptr);
+    if (s != VFEM_OK) return s;
+    CK(cudaStreamSynchronize(p->stream));
+    p->rhsSet = true;
+    return VFEM_OK;
+}
+
+vfem_status vfem_problem_set_loads(vfem_problem* p, const int64_t* nodes, const double* loads, int64_t n) {
+    if (!p || (n > 0 && (!nodes || !loads)) || n < 0) return fail(VFEM_ERR_INVALID_ARGUMENT, "null argument");
+    const int64_t nn = p->L[0].nused;
+    std::vector<double> f(3 * (size_t)nn, 0.0);
+    for (int64_t k = 0; k < n; ++k) {
+        if (nodes[k] < 0 || nodes[k] >= nn) return fail(VFEM_ERR_INVALID_ARGUMENT, "load node id out of range");
+        for (int c = 0; c < 3; ++c) f[3 * nodes[k] + c] = loads[3 * k + c];
+    }
+    return vfem_problem_set_rhs(p, f.data());
+}
+
+vfem_status vfem_solve_device(vfem_problem* p, const vfem_options* opt, double* u_out, vfem_stats* st) {
+    if (!p) return fail(VFEM_ERR_INVALID_ARGUMENT, "null problem");
+    if (!p->rhsSet) return fail(VFEM_ERR_INVALID_ARGUMENT, "right-hand side not set");
+    if (st) std::memset(st, 0, sizeof(*st));
+    vfem_status s = solveImpl(p, opt, false, st);
+    if (u_out && (s == VFEM_OK || s == VFEM_ERR_NOT_CONVERGED)) {
+        vfem_status s2 = fromDenseHost(p, 0, p->x64, u_out);
+        if (s2 != VFEM_OK) return s2;
+    }
+    return s;
+}
+
+vfem_status vfem_solve(vfem_problem* p, const vfem_options* opt, const double* u0, double* u_out, vfem_stats* st) {
+    if (!p || !u_out) return fail(VFEM_ERR_INVALID_ARGUMENT, "null argument");
+    if (!p->rhsSet) return fail(VFEM_ERR_INVALID_ARGUMENT, "right-hand side not set");
+    CK(cudaSetDevice(p->device));
+    if (st) std::memset(st, 0, sizeof(*st));
+    if (u0) {
+        vfem_status s0 = toDenseHost(p, 0, u0, p->x64, nullptr);
+        if (s0 != VFEM_OK) return s0;
+    }
+    vfem_status s = solveImpl(p, opt, u0 != nullptr, st);
+    if (s == VFEM_OK || s == VFEM_ERR_NOT_CONVERGED) {
+        vfem_status s2 = fromDenseHost(p, 0, p->x64, u_out);
+        if (s2 != VFEM_OK) return s2;
+    }
+    return s;
+}
+
+vfem_status vfem_apply_operator(vfem_problem* p, const double* x, double* y) {
+    if (!p || !x || !y) return fail(VFEM_ERR_INVALID_ARGUMENT, "null argument");
+    CK(cudaSetDevice(p->device));
+    vfem_status s = toDenseHost(p, 0, x, p->p64, nullptr);
+    if (s != VFEM_OK) return s;
+    MatvecArgs<double> a = mvArgs<double>(p, 0, p->p64, p->Ap64, MV_AX);
+    a.checkDone = 0;
+    p->launches += matvec<double>(p, a);
+    g_launches += 1;
+    CK(cudaGetLastError());
+    return fromDenseHost(p, 0, p->Ap64, y);
+}
+
+vfem_status vfem_apply_preconditioner(vfem_problem* p, int32_t mg_mode, const double* r, double* z) {
+    if (!p || !r || !z || (mg_mode != VFEM_MG_REFERENCE && mg_mode != VFEM_MG_VCYCLE))
+        return fail(VFEM_ERR_INVALID_ARGUMENT, "bad argument");
+    CK(cudaSetDevice(p->device));
+    DevLevel& l0 = p->L[0];
+    vfem_status s = toDenseHost(p, 0, r, l0.r64, nullptr);
+    if (s != VFEM_OK) return s;
+    vfem_options o;
+    vfem_options_default(&o);
+    o.mg_mode = mg_mode;
+    launchInitScalars(p->stream, p->S, 1e-6, 1, 0, 0, 0);
+    double* zo = nullptr;
+    int k = 1 + vcycle<double>(p, o, 0, l0.r64, l0.z64, &zo, nullptr, EPI_NONE);
+    p->launches += k;
+    g_launches += k;
+    CK(cudaGetLastError());
+    return fromDenseHost(p, 0, zo, z);
+}
+
+vfem_status vfem_restrict(vfem_problem* p, int32_t level, const double* fine, double* coarse) {
+    if (!p || !fine || !coarse || level < 0 || level + 1 >= (int)p->L.size())
+        return fail(VFEM_ERR_INVALID_ARGUMENT, "bad argument");
+    CK(cudaSetDevice(p->device));
+    DevLevel& lf = p->L[level];
+    DevLevel& lc = p->L[level + 1];
+    vfem_status s = toDenseHost(p, level, fine, lf.t64, nullptr);
+    if (s != VFEM_OK) return s;
+    launchInitScalars(p->stream, p->S, 1e-6, 1, 0, 0, 0);
+    int k = 1 + launchRestrict<double>(ctx(p), lf.g, lc.g, lc.div, lf.t64, lc.t64, 0);
+    p->launches += k;
+    g_launches += k;
+    CK(cudaGetLastError());
+    return fromDenseHost(p, level + 1, lc.t64, coarse);
+}
+
+vfem_status vfem_interpolate(vfem_problem* p, int32_t level, const double* coarse, double* fine) {
+    if (!p || !fine || !coarse || level < 0 || level + 1 >= (int)p->L.size())
+        return fail(VFEM_ERR_INVALID_ARGUMENT, "bad argument");
+    CK(cudaSetDevice(p->device));
+    DevLevel& lf = p->L[level];
+    DevLevel& lc = p->L[level + 1];
+    vfem_status s = toDenseHost(p, level + 1, coarse, lc.t64, nullptr);
+    if (s != VFEM_OK) return s;
+    launchInitScalars(p->stream, p->S, 1e-6, 1, 0, 0, 0);
+    CK(cudaMemsetAsync(lf.t64, 0, sizeof(double) * (size_t)lf.nvec(), p->stream));
+    // Masked trilinear prolongation only: coefficient 0 on the Jacobi term, no fixed mask
+    // (the reference's interpolate does not zero fixed nodes).
+    int k = 1 + launchProlongSmooth<double>(ctx(p), lf.g, lc.g, lc.div, lc.t64, lf.t64, lf.dinv64, lf.flags, lf.z64,
+                                            0.0, 0, nullptr, EPI_NONE, 0);
+    p->launches += k;
+    g_launches += k;
+    CK(cudaGetLastError());
+    return fromDenseHost(p, level, lf.z64, fine);
+}
+
+vfem_status vfem_inverse_diagonal(vfem_problem* p, int32_t level, double* out) {
+    if (!p || !out || level < 0 || level >= (int)p->L.size()) return fail(VFEM_ERR_INVALID_ARGUMENT, "bad argument");
+    CK(cudaSetDevice(p->device));
+    return fromDenseHost(p, level, p->L[level].dinv64, out);
+}
+
+vfem_status vfem_fixed_nodes(vfem_problem* p, int32_t level, int64_t* out, int64_t cap, int64_t* count) {
+    if (!p || level < 0 || level >= (int)p->H.L.size()) return fail(VFEM_ERR_INVALID_ARGUMENT, "bad argument");
+    const auto& f = p->H.L[level].fixedIds;
+    if (count) *count = (int64_t)f.size();
+    if (out)
+        for (int64_t i = 0; i < std::min<int64_t>(cap, (int64_t)f.size()); ++i) out[i] = f[i];
+    return VFEM_OK;
+}
+
+}  // extern "C"

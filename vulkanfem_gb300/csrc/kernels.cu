@@ -1,0 +1,820 @@
+// kernels.cu -- sm_103a kernels of the voxel MG-PCG solve.
+//
+// Kernel map (reference shader / routine it replaces, paths relative to the
+// reference project root):
+//   kMatvec          MatxVec.comp + FixedNodes.comp + VecDotVec.comp
+//                    (MatrixFreeSparse.hpp:197-214): atomic-free element-by-element
+//                    product on a 2.5-D tile, fixed rows zeroed, dots fused.
+//   kRestrict        CWiseMult.comp + Restrict.comp (MultigridPreconditioner.hpp:67-108):
+//                    full weighting on the dense grid, one thread per coarse node.
+//   kProlongSmooth   Interpolate.comp + PreSmoothAndAXPY.comp + Smooth.comp
+//                    (MultigridPreconditioner.hpp:110-155,176-181), fixed mask and r.z fused.
+//   kCoarseGather/kGemv  the coarsest SimplicialLDLT solve (MultigridPreconditioner.hpp:174-175)
+//                    as a dense inverse applied on the device.
+//   kUpdateXR        ConjugateGradient_1.comp + VecDotVec.comp (r.r).
+//   kUpdateP         ConjugateGradient_2.comp.
+// Reductions are deterministic: block partials in a fixed grid, summed in a
+// fixed order by the last block to finish (no floating-point atomics).
+#include <cfloat>
+#include <cstdio>
+
+#include "kernels.h"
+
+namespace vfem {
+
+namespace {
+
+constexpr int MV_TX = 32, MV_TY = 8, MV_ZC = 16;
+constexpr int NT = 256;
+constexpr int PZ = 8;  // z nodes per thread in the per-node kernels
+
+__device__ __forceinline__ double warpSum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Deterministic block + grid reduction of K sums.  Returns true in thread 0 of
+// the last block to finish, with the totals in tot.  NTH = threads per block.
+template <int NTH, int K>
+__device__ __forceinline__ bool gridReduce(double (&v)[K], const RedBuf& rb, double (&tot)[K]) {
+    __shared__ double sred[K][NTH / 32];
+    __shared__ int amLast;
+    const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+    const int lane = tid & 31, warp = tid >> 5;
+    const unsigned nb = gridDim.x * gridDim.y * gridDim.z;
+    const unsigned bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        double s = warpSum(v[k]);
+        if (lane == 0) sred[k][warp] = s;
+    }
+    __syncthreads();
+    if (tid == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            double s = 0;
+            for (int w = 0; w < NTH / 32; ++w) s += sred[k][w];
+            rb.partials[(size_t)k * kMaxRedBlocks + bid] = s;
+        }
+        __threadfence();
+        unsigned t = atomicAdd(rb.ticket, 1u);
+        amLast = (t == nb - 1);
+    }
+    __syncthreads();
+    if (!amLast) return false;
+    __threadfence();
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        double s = 0;
+        for (unsigned i = tid; i < nb; i += NTH) s += __ldcg(&rb.partials[(size_t)k * kMaxRedBlocks + i]);
+        s = warpSum(s);
+        if (lane == 0) sred[k][warp] = s;
+    }
+    __syncthreads();
+    if (tid == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            double s = 0;
+            for (int w = 0; w < NTH / 32; ++w) s += sred[k][w];
+            tot[k] = s;
+        }
+        *rb.ticket = 0u;
+    }
+    return tid == 0;
+}
+
+__device__ void applyEpi(int epi, Scalars* S, double t0, double t1) {
+    switch (epi) {
+        case EPI_STORE:
+            S->red0 = t0;
+            S->red1 = t1;
+            break;
+        case EPI_ALPHA:
+            S->pAp = t0;
+            S->matvecs++;
+            if (!(t0 > 0.0) || !isfinite(t0)) S->done = BREAKDOWN;
+            else S->alpha = S->rho / t0;
+            break;
+        case EPI_CONV:
+            S->rr = t0;
+            if (!isfinite(t0)) S->done = BREAKDOWN;
+            else if (t0 < S->threshold) {
+                if (S->mixed) S->checkPending = 1;
+                else S->done = CONVERGED;
+            }
+            break;
+        case EPI_RHO0:
+            S->rho = t0;
+            if (!isfinite(t0)) S->done = BREAKDOWN;
+            break;
+        case EPI_BETA:
+            S->rhoOld = S->rho;
+            S->rho = t0;
+            S->zAp = t1;
+            S->beta = S->flexible ? -t1 / S->pAp : t0 / S->rhoOld;
+            S->iter++;
+            if (!isfinite(S->beta)) S->done = BREAKDOWN;
+            else if (S->iter >= S->maxIter) S->done = MAXITER;
+            break;
+        case EPI_INIT:
+            S->rhsNorm2 = t0;
+            S->rr = t1;
+            S->threshold = fmax(S->tol2 * t0, DBL_MIN);
+            if (t0 == 0.0 || t1 < S->threshold) S->done = CONVERGED;
+            break;
+        case EPI_TRUE:
+            S->rrTrue = t0;
+            S->rr = t0;
+            S->checkPending = 0;
+            S->replacements++;
+            if (!isfinite(t0)) S->done = BREAKDOWN;
+            else if (t0 < S->threshold) S->done = CONVERGED;
+            break;
+        default:
+            break;
+    }
+}
+
+__device__ __forceinline__ bool trueResidualDue(const Scalars* S) {
+    return S->checkPending || (S->replaceEvery > 0 && S->iter > 0 && (S->iter % S->replaceEvery) == 0);
+}
+
+template <typename T>
+struct Ks {
+    T v[45];
+};
+template <typename T>
+struct Kd {
+    T v[576];
+};
+
+// In-place 8-point Walsh-Hadamard transform of each displacement component:
+// v[3m+c] = sum_a (-1)^popcount(m&a) u[3a+c].
+template <typename T>
+__device__ __forceinline__ void fwht8x3(T (&v)[24]) {
+#pragma unroll
+    for (int s = 1; s < 8; s <<= 1) {
+#pragma unroll
+        for (int a = 0; a < 8; ++a) {
+            if (a & s) continue;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                T p = v[3 * a + c], q = v[3 * (a + s) + c];
+                v[3 * a + c] = p + q;
+                v[3 * (a + s) + c] = p - q;
+            }
+        }
+    }
+}
+
+// y = e * Ke u for an isotropic cube element: Ke = H^T Khat H with Khat on the
+// 45-entry pattern (8 symmetry classes), H the per-component Walsh-Hadamard
+// transform.  ~190 flops instead of 1152 for the dense 24x24 product.
+template <typename T>
+__device__ __forceinline__ void elemStruct(T (&u)[24], T (&y)[24], const Ks<T>& k, T e) {
+    fwht8x3(u);
+#pragma unroll
+    for (int i = 3; i < 24; ++i) u[i] *= e;
+#pragma unroll
+    for (int i = 0; i < 24; ++i) y[i] = T(0);
+#define KS_(n, r, c) y[r] = fma(k.v[n], u[c], y[r]);
+    KS_(0, 3, 3) KS_(1, 3, 7) KS_(2, 3, 14) KS_(3, 7, 3) KS_(4, 7, 7) KS_(5, 7, 14) KS_(6, 14, 3) KS_(7, 14, 7)
+    KS_(8, 14, 14)
+    KS_(9, 6, 6) KS_(10, 6, 4) KS_(11, 4, 6) KS_(12, 4, 4) KS_(13, 23, 23)
+    KS_(14, 12, 12) KS_(15, 12, 5) KS_(16, 5, 12) KS_(17, 5, 5) KS_(18, 22, 22)
+    KS_(19, 13, 13) KS_(20, 13, 8) KS_(21, 8, 13) KS_(22, 8, 8) KS_(23, 21, 21)
+    KS_(24, 10, 10) KS_(25, 10, 17) KS_(26, 17, 10) KS_(27, 17, 17)
+    KS_(28, 9, 9) KS_(29, 9, 20) KS_(30, 20, 9) KS_(31, 20, 20)
+    KS_(32, 15, 15) KS_(33, 15, 19) KS_(34, 19, 15) KS_(35, 19, 19)
+    KS_(36, 18, 18) KS_(37, 18, 16) KS_(38, 18, 11) KS_(39, 16, 18) KS_(40, 16, 16) KS_(41, 16, 11)
+    KS_(42, 11, 18) KS_(43, 11, 16) KS_(44, 11, 11)
+#undef KS_
+    fwht8x3(y);
+}
+
+// y = e * Ke u, general symmetric Ke.
+template <typename T>
+__device__ __forceinline__ void elemDense(const T (&u)[24], T (&y)[24], const Kd<T>& k, T e) {
+#pragma unroll
+    for (int r = 0; r < 24; ++r) {
+        T s = T(0);
+#pragma unroll
+        for (int c = 0; c < 24; ++c) s = fma(k.v[r * 24 + c], u[c], s);
+        y[r] = s * e;
+    }
+}
+
+template <typename T, bool STRUCT>
+struct KP;
+template <typename T>
+struct KP<T, true> {
+    typedef Ks<T> type;
+};
+template <typename T>
+struct KP<T, false> {
+    typedef Kd<T> type;
+};
+
+constexpr int kSuElems = 2 * (MV_TY + 1) * (MV_TX + 1) * 3;
+constexpr int kSyElems = MV_TY * MV_TX * 18;
+
+// Element-by-element product on a 2.5-D tile.  A block of 32 x 8 threads marches
+// up a z-range; at each element layer thread (tx,ty) computes the element whose
+// lower corner is node (x0+tx-1, y0+ty-1) and owns node (x0+tx, y0+ty), which is
+// the (1,1) corner of its own element and a corner of the three neighbouring
+// threads' elements.  Element outputs pass through shared memory once; each
+// owned node sums its four in-layer contributions for the bottom face (node
+// layer k) and the top face (node layer k+1), so no atomics are needed.
+template <typename T, bool STRUCT>
+__global__ void __launch_bounds__(MV_TX* MV_TY)
+    kMatvec(MatvecArgs<T> a, const typename KP<T, STRUCT>::type kp, Scalars* S, RedBuf rb) {
+    if (a.checkDone && S->done) return;
+    if (a.condTrue && !trueResidualDue(S)) return;
+    extern __shared__ __align__(16) unsigned char smemRaw[];
+    T* su = reinterpret_cast<T*>(smemRaw);
+    T* sy = su + kSuElems;
+    const Grid g = a.g;
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * MV_TX + tx;
+    const int x0 = blockIdx.x * (MV_TX - 1), y0 = blockIdx.y * (MV_TY - 1), z0 = blockIdx.z * MV_ZC;
+    const int zend = min(z0 + MV_ZC, g.nz);
+    const int ecx = x0 + tx - 1, ecy = y0 + ty - 1;
+    const int onx = x0 + tx, ony = y0 + ty;
+    const bool owner = (tx < MV_TX - 1) && (ty < MV_TY - 1) && onx < g.nx && ony < g.ny;
+    const bool ecxy = ecx >= 0 && ecx < g.ex && ecy >= 0 && ecy < g.ey;
+    const T sc = (T)a.scale;
+#define SU(b, iy, ix, c) su[((((b) * (MV_TY + 1)) + (iy)) * (MV_TX + 1) + (ix)) * 3 + (c)]
+#define SY(iy, ix, k) sy[((iy) * MV_TX + (ix)) * 18 + (k)]
+    auto load = [&](int zl) {
+        const int b = zl & 1;
+        for (int i = tid; i < (MV_TX + 1) * (MV_TY + 1); i += MV_TX * MV_TY) {
+            const int ix = i % (MV_TX + 1), iy = i / (MV_TX + 1);
+            const int gx = x0 - 1 + ix, gy = y0 - 1 + iy;
+            T v0 = T(0), v1 = T(0), v2 = T(0);
+            if (gx >= 0 && gx < g.nx && gy >= 0 && gy < g.ny && zl >= 0 && zl < g.nz) {
+                const T* p = a.x + 3 * g.store(gx, gy, zl);
+                v0 = p[0];
+                v1 = p[1];
+                v2 = p[2];
+            }
+            SU(b, iy, ix, 0) = v0;
+            SU(b, iy, ix, 1) = v1;
+            SU(b, iy, ix, 2) = v2;
+        }
+    };
+    T acc[3] = {T(0), T(0), T(0)};
+    double d0 = 0.0, d1 = 0.0;
+    load(z0 - 1);
+    for (int k = z0 - 1; k < zend; ++k) {
+        load(k + 1);
+        __syncthreads();
+        T ye[24];
+        float Ee = 0.f;
+        if (ecxy && k >= 0 && k < g.ez) Ee = a.E[g.store(ecx, ecy, k)];
+        if (Ee != 0.f) {
+            T u[24];
+#pragma unroll
+            for (int n = 0; n < 8; ++n) {
+                const int dx = n & 1, dy = (n >> 1) & 1, dz = n >> 2;
+                const int b = (k + dz) & 1;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) u[3 * n + c] = SU(b, ty + dy, tx + dx, c);
+            }
+            if constexpr (STRUCT) elemStruct<T>(u, ye, kp, sc * (T)Ee);
+            else elemDense<T>(u, ye, kp, sc * (T)Ee);
+        } else {
+#pragma unroll
+            for (int i = 0; i < 24; ++i) ye[i] = T(0);
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            SY(ty, tx, 0 + c) = ye[0 + c];    // a = 0
+            SY(ty, tx, 3 + c) = ye[3 + c];    // a = 1
+            SY(ty, tx, 6 + c) = ye[6 + c];    // a = 2
+            SY(ty, tx, 9 + c) = ye[12 + c];   // a = 4
+            SY(ty, tx, 12 + c) = ye[15 + c];  // a = 5
+            SY(ty, tx, 15 + c) = ye[18 + c];  // a = 6
+        }
+        __syncthreads();
+        if (owner) {
+            T lo[3], hi[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                lo[c] = ye[9 + c] + SY(ty, tx + 1, 6 + c) + SY(ty + 1, tx, 3 + c) + SY(ty + 1, tx + 1, 0 + c);
+                hi[c] = ye[21 + c] + SY(ty, tx + 1, 15 + c) + SY(ty + 1, tx, 12 + c) + SY(ty + 1, tx + 1, 9 + c);
+            }
+            if (k >= z0) {
+                const int64_t s = g.store(onx, ony, k);
+                const uint8_t fl = a.flags[s];
+                const bool fixed = (fl & FLAG_FIXED) != 0;
+                const int b = k & 1;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const T ax = fixed ? T(0) : acc[c] + lo[c];
+                    T out;
+                    T fv = T(0);
+                    if (a.mode != MV_AX) fv = a.f[3 * s + c];
+                    const T xv = SU(b, ty + 1, tx + 1, c);
+                    switch (a.mode) {
+                        case MV_AX: out = ax; break;
+                        case MV_RESID: out = fv - ax; break;
+                        case MV_RESID0: out = fixed ? T(0) : fv - ax; break;
+                        default: out = fixed ? T(0) : xv + (T)a.omega * a.dinv[3 * s + c] * (fv - ax); break;
+                    }
+                    a.y[3 * s + c] = out;
+                    if (a.y32) a.y32[3 * s + c] = (float)out;
+                    if (a.dot0 == DOT_X_OUT) d0 += (double)xv * (double)out;
+                    else if (a.dot0 == DOT_OUT_OUT) d0 += (double)out * (double)out;
+                    else if (a.dot0 == DOT_F_OUT) d0 += (double)fv * (double)out;
+                    if (a.dot1) d1 += (double)out * (double)a.aux[3 * s + c];
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < 3; ++c) acc[c] = hi[c];
+        }
+    }
+#undef SU
+#undef SY
+    if (a.epi != EPI_NONE) {
+        double v[2] = {d0, d1}, t[2];
+        if (gridReduce<MV_TX * MV_TY, 2>(v, rb, t)) applyEpi(a.epi, S, t[0], t[1]);
+    }
+}
+
+// Full weighting (the transpose of trilinear prolongation) on the dense grid:
+// rc[C] = sum_{|d| < DIV} prod_i (DIV - |d_i|)/DIV * rf[DIV*C + d].  Equal to
+// the reference's W-weighted per-element restriction (see setup.cpp).
+template <typename T, int DIV>
+__global__ void __launch_bounds__(256) kRestrict(Grid gf, Grid gc, const T* __restrict__ rf, T* __restrict__ rc,
+                                                 const Scalars* S, int checkDone) {
+    if (checkDone && S->done) return;
+    const int cx = blockIdx.x * 32 + threadIdx.x, cy = blockIdx.y * 8 + threadIdx.y;
+    if (cx >= gc.nx || cy >= gc.ny) return;
+    constexpr int R = DIV - 1;
+    const T inv = T(1) / T(DIV);
+    for (int cz = blockIdx.z * PZ; cz < min(gc.nz, (int)(blockIdx.z + 1) * PZ); ++cz) {
+        T a0 = T(0), a1 = T(0), a2 = T(0);
+        for (int dz = -R; dz <= R; ++dz) {
+            const int fz = cz * DIV + dz;
+            if (fz < 0 || fz >= gf.nz) continue;
+            const T wz = T(DIV - abs(dz)) * inv;
+            for (int dy = -R; dy <= R; ++dy) {
+                const int fy = cy * DIV + dy;
+                if (fy < 0 || fy >= gf.ny) continue;
+                const T wy = T(DIV - abs(dy)) * inv;
+                T s0 = T(0), s1 = T(0), s2 = T(0);
+#pragma unroll
+                for (int dx = -R; dx <= R; ++dx) {
+                    const int fx = cx * DIV + dx;
+                    if (fx < 0 || fx >= gf.nx) continue;
+                    const T wx = T(DIV - abs(dx)) * inv;
+                    const T* p = rf + 3 * gf.store(fx, fy, fz);
+                    s0 = fma(wx, p[0], s0);
+                    s1 = fma(wx, p[1], s1);
+                    s2 = fma(wx, p[2], s2);
+                }
+                const T w = wz * wy;
+                a0 = fma(w, s0, a0);
+                a1 = fma(w, s1, a1);
+                a2 = fma(w, s2, a2);
+            }
+        }
+        T* q = rc + 3 * gc.store(cx, cy, cz);
+        q[0] = a0;
+        q[1] = a1;
+        q[2] = a2;
+    }
+}
+
+// Trilinear prolongation of coarse node values to fine node (fx,fy,fz).
+template <typename T, int DIV>
+__device__ __forceinline__ void prolongAt(const Grid& gf, const Grid& gc, const T* zc, int fx, int fy, int fz,
+                                          T (&acc)[3]) {
+    const int px = fx / DIV, py = fy / DIV, pz = fz / DIV;
+    const int rx = fx - px * DIV, ry = fy - py * DIV, rz = fz - pz * DIV;
+    const T inv = T(1) / T(DIV);
+    acc[0] = acc[1] = acc[2] = T(0);
+#pragma unroll
+    for (int iz = 0; iz < 2; ++iz) {
+        if (iz && rz == 0) continue;
+        const T wz = iz ? T(rz) * inv : T(DIV - rz) * inv;
+#pragma unroll
+        for (int iy = 0; iy < 2; ++iy) {
+            if (iy && ry == 0) continue;
+            const T wy = iy ? T(ry) * inv : T(DIV - ry) * inv;
+#pragma unroll
+            for (int ix = 0; ix < 2; ++ix) {
+                if (ix && rx == 0) continue;
+                const T wx = ix ? T(rx) * inv : T(DIV - rx) * inv;
+                const T w = wz * wy * wx;
+                const T* p = zc + 3 * gc.store(px + ix, py + iy, pz + iz);
+                acc[0] = fma(w, p[0], acc[0]);
+                acc[1] = fma(w, p[1], acc[1]);
+                acc[2] = fma(w, p[2], acc[2]);
+            }
+        }
+    }
+}
+
+// Reference-mode up-leg of the V-cycle: zf = P zc + coef * dinv o rf on used
+// nodes (coef = 2: the down-leg and up-leg Jacobi steps of the reference, which
+// never update r), 0 elsewhere; fixed nodes zeroed on the finest level.
+template <typename T, int DIV>
+__global__ void __launch_bounds__(256)
+    kProlongSmooth(Grid gf, Grid gc, const T* __restrict__ zc, const T* __restrict__ rf, const T* __restrict__ dinv,
+                   const uint8_t* __restrict__ flags, T* __restrict__ zf, double coef, int maskFixed,
+                   const T* __restrict__ aux, int epi, Scalars* S, RedBuf rb, int checkDone) {
+    if (checkDone && S->done) return;
+    const int fx = blockIdx.x * 32 + threadIdx.x, fy = blockIdx.y * 8 + threadIdx.y;
+    const bool valid = fx < gf.nx && fy < gf.ny;
+    double d0 = 0.0, d1 = 0.0;
+    if (valid) {
+        for (int fz = blockIdx.z * PZ; fz < min(gf.nz, (int)(blockIdx.z + 1) * PZ); ++fz) {
+            const int64_t s = gf.store(fx, fy, fz);
+            const uint8_t fl = flags[s];
+            T out[3] = {T(0), T(0), T(0)};
+            T r[3] = {T(0), T(0), T(0)};
+            if (fl & FLAG_USED) {
+                T acc[3];
+                prolongAt<T, DIV>(gf, gc, zc, fx, fy, fz, acc);
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    r[c] = rf[3 * s + c];
+                    out[c] = acc[c] + (T)coef * dinv[3 * s + c] * r[c];
+                }
+                if (maskFixed && (fl & FLAG_FIXED)) out[0] = out[1] = out[2] = T(0);
+            }
+#pragma unroll
+            for (int c = 0; c < 3; ++c) zf[3 * s + c] = out[c];
+            if (epi != EPI_NONE) {
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    d0 += (double)r[c] * (double)out[c];
+                    if (aux) d1 += (double)out[c] * (double)aux[3 * s + c];
+                }
+            }
+        }
+    }
+    if (epi != EPI_NONE) {
+        double v[2] = {d0, d1}, t[2];
+        if (gridReduce<256, 2>(v, rb, t)) applyEpi(epi, S, t[0], t[1]);
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) kJacobiZero(int64_t nnode, const T* __restrict__ r, const T* __restrict__ dinv,
+                                                   const uint8_t* __restrict__ flags, T* __restrict__ z, double omega,
+                                                   const Scalars* S, int checkDone) {
+    if (checkDone && S->done) return;
+    for (int64_t s = blockIdx.x * (int64_t)NT + threadIdx.x; s < nnode; s += (int64_t)gridDim.x * NT) {
+        const uint8_t fl = flags[s];
+        const bool act = (fl & FLAG_USED) && !(fl & FLAG_FIXED);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) z[3 * s + c] = act ? (T)omega * dinv[3 * s + c] * r[3 * s + c] : T(0);
+    }
+}
+
+template <typename T, int DIV>
+__global__ void __launch_bounds__(256) kProlongAdd(Grid gf, Grid gc, const T* __restrict__ zc,
+                                                   const uint8_t* __restrict__ flags, T* __restrict__ zf,
+                                                   const Scalars* S, int checkDone) {
+    if (checkDone && S->done) return;
+    const int fx = blockIdx.x * 32 + threadIdx.x, fy = blockIdx.y * 8 + threadIdx.y;
+    if (fx >= gf.nx || fy >= gf.ny) return;
+    for (int fz = blockIdx.z * PZ; fz < min(gf.nz, (int)(blockIdx.z + 1) * PZ); ++fz) {
+        const int64_t s = gf.store(fx, fy, fz);
+        const uint8_t fl = flags[s];
+        if (!(fl & FLAG_USED) || (fl & FLAG_FIXED)) continue;
+        T acc[3];
+        prolongAt<T, DIV>(gf, gc, zc, fx, fy, fz, acc);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) zf[3 * s + c] += acc[c];
+    }
+}
+
+template <typename T>
+__global__ void kCoarseGather(int64_t n, const int32_t* __restrict__ freeDof, const T* __restrict__ rc,
+                              T* __restrict__ b, const Scalars* S, int checkDone) {
+    if (checkDone && S->done) return;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        b[i] = rc[freeDof[i]];
+}
+
+// y = Kinv b, one warp per row; results scattered to the coarse free DOFs.
+template <typename T>
+__global__ void __launch_bounds__(256) kGemv(const T* __restrict__ K, int64_t n, const T* __restrict__ b,
+                                             const int32_t* __restrict__ freeDof, T* __restrict__ zc,
+                                             const Scalars* S, int checkDone) {
+    if (checkDone && S->done) return;
+    const int lane = threadIdx.x & 31;
+    const int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (row >= n) return;
+    const T* k = K + row * n;
+    T acc = T(0);
+    for (int64_t j = lane; j < n; j += 32) acc = fma(k[j], b[j], acc);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) zc[freeDof[row]] = acc;
+}
+
+template <typename TX, typename TV>
+__global__ void __launch_bounds__(256) kUpdateXR(int64_t n, TX* __restrict__ x, TV* __restrict__ r,
+                                                 const TV* __restrict__ p, const TV* __restrict__ Ap, Scalars* S,
+                                                 RedBuf rb) {
+    if (S->done) return;
+    const double alpha = S->alpha;
+    const TV av = (TV)alpha;
+    double acc = 0.0;
+    TV part = TV(0);
+    int cnt = 0;
+    for (int64_t i = blockIdx.x * (int64_t)NT + threadIdx.x; i < n; i += (int64_t)gridDim.x * NT) {
+        const TV pi = p[i], api = Ap[i];
+        x[i] = (TX)((TX)x[i] + (TX)alpha * (TX)pi);
+        const TV ri = r[i] - av * api;
+        r[i] = ri;
+        part = fma(ri, ri, part);
+        if (++cnt == 8) {  // short partial sums in the vector type, accumulated in FP64
+            acc += (double)part;
+            part = TV(0);
+            cnt = 0;
+        }
+    }
+    acc += (double)part;
+    double v[1] = {acc}, t[1];
+    if (gridReduce<NT, 1>(v, rb, t)) applyEpi(EPI_CONV, S, t[0], 0.0);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) kUpdateP(int64_t n, T* __restrict__ p, const T* __restrict__ z,
+                                                const Scalars* S, int first) {
+    if (S->done) return;
+    const T beta = first ? T(0) : (T)S->beta;
+    for (int64_t i = blockIdx.x * (int64_t)NT + threadIdx.x; i < n; i += (int64_t)gridDim.x * NT)
+        p[i] = first ? z[i] : fma(beta, p[i], z[i]);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) kDots(int64_t n, const T* __restrict__ a, const T* __restrict__ b,
+                                             const T* __restrict__ c, const T* __restrict__ d, int epi, Scalars* S,
+                                             RedBuf rb, int checkDone) {
+    if (checkDone && S->done) return;
+    double s0 = 0.0, s1 = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)NT + threadIdx.x; i < n; i += (int64_t)gridDim.x * NT) {
+        if (a) s0 += (double)a[i] * (double)b[i];
+        if (c) s1 += (double)c[i] * (double)d[i];
+    }
+    double v[2] = {s0, s1}, t[2];
+    if (gridReduce<NT, 2>(v, rb, t)) applyEpi(epi, S, t[0], t[1]);
+}
+
+template <typename TI, typename TO>
+__global__ void kConvert(int64_t n, const TI* __restrict__ x, TO* __restrict__ y) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        y[i] = (TO)x[i];
+}
+
+template <typename T>
+__global__ void kFill(int64_t n, T* __restrict__ y, T v) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        y[i] = v;
+}
+
+template <typename T>
+__global__ void kScatterCompressed(int64_t nn, const int32_t* __restrict__ store, const double* __restrict__ comp,
+                                   T* __restrict__ dense) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < 3 * nn; i += (int64_t)gridDim.x * blockDim.x)
+        dense[3 * (int64_t)store[i / 3] + i % 3] = (T)comp[i];
+}
+
+template <typename T>
+__global__ void kGatherCompressed(int64_t nn, const int32_t* __restrict__ store, const T* __restrict__ dense,
+                                  double* __restrict__ comp) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < 3 * nn; i += (int64_t)gridDim.x * blockDim.x)
+        comp[i] = (double)dense[3 * (int64_t)store[i / 3] + i % 3];
+}
+
+// One parity colour of the coarsest-matrix assembly: same-colour elements share
+// no node, so plain += is race-free and the summation order is fixed.
+__global__ void kAssembleCoarse(Grid g, const float* __restrict__ E, const int32_t* __restrict__ freeNode,
+                                const Kd<double> ke, double scale, double* __restrict__ K, int64_t n, int color) {
+    const int hx = (g.ex + 1 - (color & 1)) / 2, hy = (g.ey + 1 - ((color >> 1) & 1)) / 2;
+    const int64_t e = blockIdx.x;
+    const int ix = (int)(e % hx), iy = (int)((e / hx) % hy), iz = (int)(e / ((int64_t)hx * hy));
+    const int x = 2 * ix + (color & 1), y = 2 * iy + ((color >> 1) & 1), z = 2 * iz + (color >> 2);
+    if (x >= g.ex || y >= g.ey || z >= g.ez) return;
+    const float Ee = E[g.store(x, y, z)];
+    if (Ee == 0.f) return;
+    for (int ent = threadIdx.x; ent < 576; ent += blockDim.x) {
+        const int r = ent / 24, c = ent % 24;
+        const int a = r / 3, ci = r % 3, b = c / 3, cj = c % 3;
+        const int32_t na = freeNode[g.store(x + (a & 1), y + ((a >> 1) & 1), z + (a >> 2))];
+        const int32_t nb = freeNode[g.store(x + (b & 1), y + ((b >> 1) & 1), z + (b >> 2))];
+        if (na < 0 || nb < 0) continue;
+        K[(3 * (int64_t)na + ci) * n + 3 * (int64_t)nb + cj] += scale * (double)Ee * ke.v[ent];
+    }
+}
+
+__global__ void kSymmetrize(double* K, int64_t n) {
+    // Column-major lower triangle (cuSOLVER) == row-major upper triangle: copy it down.
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n * n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = i / n, c = i % n;
+        if (c < r) K[i] = K[c * n + r];
+    }
+}
+
+__global__ void kInitScalars(Scalars* S, double tol, long long maxIter, int flexible, int mixed, int replaceEvery) {
+    Scalars s = {};
+    s.tol2 = tol * tol;
+    s.maxIter = maxIter;
+    s.flexible = flexible;
+    s.mixed = mixed;
+    s.replaceEvery = replaceEvery;
+    *S = s;
+}
+
+inline int flatBlocks(int64_t n) {
+    int64_t b = (n + NT - 1) / NT;
+    if (b > 152 * 8) b = 152 * 8;
+    if (b < 1) b = 1;
+    return (int)b;
+}
+
+inline dim3 nodeGrid(const Grid& g) {
+    return dim3((g.nx + 31) / 32, (g.ny + 7) / 8, (g.nz + PZ - 1) / PZ);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ launchers
+
+cudaError_t setKernelAttributes() {
+    const int s64 = (kSuElems + kSyElems) * (int)sizeof(double), s32 = (kSuElems + kSyElems) * (int)sizeof(float);
+    cudaError_t e;
+    if ((e = cudaFuncSetAttribute(kMatvec<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, s64))) return e;
+    if ((e = cudaFuncSetAttribute(kMatvec<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, s64))) return e;
+    if ((e = cudaFuncSetAttribute(kMatvec<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, s32))) return e;
+    return cudaFuncSetAttribute(kMatvec<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, s32);
+}
+
+template <typename T>
+int launchMatvec(const LaunchCtx& c, const MatvecArgs<T>& a, bool structured, const void* opconst) {
+    const Grid& g = a.g;
+    dim3 grid((g.nx + MV_TX - 2) / (MV_TX - 1), (g.ny + MV_TY - 2) / (MV_TY - 1), (g.nz + MV_ZC - 1) / MV_ZC);
+    dim3 block(MV_TX, MV_TY);
+    size_t smem = (size_t)(kSuElems + kSyElems) * sizeof(T);
+    if (structured) {
+        Ks<T> k;
+        const T* src = static_cast<const T*>(opconst);
+        for (int i = 0; i < 45; ++i) k.v[i] = src[i];
+        kMatvec<T, true><<<grid, block, smem, c.stream>>>(a, k, c.S, c.rb);
+    } else {
+        Kd<T> k;
+        const T* src = static_cast<const T*>(opconst) + 45;
+        for (int i = 0; i < 576; ++i) k.v[i] = src[i];
+        kMatvec<T, false><<<grid, block, smem, c.stream>>>(a, k, c.S, c.rb);
+    }
+    return 1;
+}
+
+template <typename T>
+int launchRestrict(const LaunchCtx& c, const Grid& gf, const Grid& gc, int div, const T* rf, T* rc, int checkDone) {
+    dim3 grid = nodeGrid(gc), block(32, 8);
+    if (div == 4) kRestrict<T, 4><<<grid, block, 0, c.stream>>>(gf, gc, rf, rc, c.S, checkDone);
+    else kRestrict<T, 2><<<grid, block, 0, c.stream>>>(gf, gc, rf, rc, c.S, checkDone);
+    return 1;
+}
+
+template <typename T>
+int launchProlongSmooth(const LaunchCtx& c, const Grid& gf, const Grid& gc, int div, const T* zc, const T* rf,
+                        const T* dinv, const uint8_t* flags, T* zf, double coef, int maskFixed, const T* aux, int epi,
+                        int checkDone) {
+    dim3 grid = nodeGrid(gf), block(32, 8);
+    if (div == 4)
+        kProlongSmooth<T, 4><<<grid, block, 0, c.stream>>>(gf, gc, zc, rf, dinv, flags, zf, coef, maskFixed, aux, epi,
+                                                             c.S, c.rb, checkDone);
+    else
+        kProlongSmooth<T, 2><<<grid, block, 0, c.stream>>>(gf, gc, zc, rf, dinv, flags, zf, coef, maskFixed, aux, epi,
+                                                             c.S, c.rb, checkDone);
+    return 1;
+}
+
+template <typename T>
+int launchJacobiZero(const LaunchCtx& c, const Grid& g, const T* r, const T* dinv, const uint8_t* flags, T* z,
+                     double omega, int checkDone) {
+    kJacobiZero<T><<<flatBlocks(g.nnode), NT, 0, c.stream>>>(g.nnode, r, dinv, flags, z, omega, c.S, checkDone);
+    return 1;
+}
+
+template <typename T>
+int launchProlongAdd(const LaunchCtx& c, const Grid& gf, const Grid& gc, int div, const T* zc, const uint8_t* flags,
+                     T* zf, int checkDone) {
+    dim3 grid = nodeGrid(gf), block(32, 8);
+    if (div == 4) kProlongAdd<T, 4><<<grid, block, 0, c.stream>>>(gf, gc, zc, flags, zf, c.S, checkDone);
+    else kProlongAdd<T, 2><<<grid, block, 0, c.stream>>>(gf, gc, zc, flags, zf, c.S, checkDone);
+    return 1;
+}
+
+template <typename T>
+int launchCoarseSolve(const LaunchCtx& c, const T* Kinv, int64_t n, const int32_t* freeDof, const T* rc, T* tmp, T* zc,
+                      int checkDone) {
+    if (n <= 0) return 0;
+    kCoarseGather<T><<<(int)((n + 255) / 256), 256, 0, c.stream>>>(n, freeDof, rc, tmp, c.S, checkDone);
+    kGemv<T><<<(int)((n * 32 + 255) / 256), 256, 0, c.stream>>>(Kinv, n, tmp, freeDof, zc, c.S, checkDone);
+    return 2;
+}
+
+template <typename TX, typename TV>
+int launchUpdateXR(const LaunchCtx& c, int64_t n, TX* x, TV* r, const TV* p, const TV* Ap) {
+    kUpdateXR<TX, TV><<<flatBlocks(n), NT, 0, c.stream>>>(n, x, r, p, Ap, c.S, c.rb);
+    return 1;
+}
+
+template <typename T>
+int launchUpdateP(const LaunchCtx& c, int64_t n, T* p, const T* z, int first) {
+    kUpdateP<T><<<flatBlocks(n), NT, 0, c.stream>>>(n, p, z, c.S, first);
+    return 1;
+}
+
+template <typename T>
+int launchDots(const LaunchCtx& c, int64_t n, const T* a, const T* b, const T* cc, const T* d, int epi, int checkDone) {
+    kDots<T><<<flatBlocks(n), NT, 0, c.stream>>>(n, a, b, cc, d, epi, c.S, c.rb, checkDone);
+    return 1;
+}
+
+template <typename TI, typename TO>
+int launchConvert(cudaStream_t s, int64_t n, const TI* x, TO* y) {
+    kConvert<TI, TO><<<flatBlocks(n), NT, 0, s>>>(n, x, y);
+    return 1;
+}
+
+template <typename T>
+int launchFill(cudaStream_t s, int64_t n, T* y, T v) {
+    kFill<T><<<flatBlocks(n), NT, 0, s>>>(n, y, v);
+    return 1;
+}
+
+template <typename T>
+int launchScatterCompressed(cudaStream_t s, int64_t nn, const int32_t* store, const double* comp, T* dense) {
+    kScatterCompressed<T><<<flatBlocks(3 * nn), NT, 0, s>>>(nn, store, comp, dense);
+    return 1;
+}
+
+template <typename T>
+int launchGatherCompressed(cudaStream_t s, int64_t nn, const int32_t* store, const T* dense, double* comp) {
+    kGatherCompressed<T><<<flatBlocks(3 * nn), NT, 0, s>>>(nn, store, dense, comp);
+    return 1;
+}
+
+int launchAssembleCoarse(cudaStream_t s, const Grid& g, const float* E, const int32_t* freeNode, const double* Ke,
+                         double scale, double* K, int64_t n) {
+    Kd<double> k;
+    for (int i = 0; i < 576; ++i) k.v[i] = Ke[i];
+    int launches = 0;
+    for (int color = 0; color < 8; ++color) {
+        const int hx = (g.ex + 1 - (color & 1)) / 2, hy = (g.ey + 1 - ((color >> 1) & 1)) / 2,
+                  hz = (g.ez + 1 - (color >> 2)) / 2;
+        const int64_t ne = (int64_t)hx * hy * hz;
+        if (ne <= 0) continue;
+        kAssembleCoarse<<<(unsigned)ne, 64, 0, s>>>(g, E, freeNode, k, scale, K, n, color);
+        ++launches;
+    }
+    return launches;
+}
+
+int launchSymmetrizeLowerToFull(cudaStream_t s, double* K, int64_t n) {
+    kSymmetrize<<<flatBlocks(n * n), NT, 0, s>>>(K, n);
+    return 1;
+}
+
+int launchInitScalars(cudaStream_t s, Scalars* S, double tol, long long maxIter, int flexible, int mixed,
+                      int replaceEvery) {
+    kInitScalars<<<1, 1, 0, s>>>(S, tol, maxIter, flexible, mixed, replaceEvery);
+    return 1;
+}
+
+// ------------------------------------------------------------------ instantiations
+#define INST_T(T)                                                                                                     \
+    template int launchMatvec<T>(const LaunchCtx&, const MatvecArgs<T>&, bool, const void*);                         \
+    template int launchRestrict<T>(const LaunchCtx&, const Grid&, const Grid&, int, const T*, T*, int);               \
+    template int launchProlongSmooth<T>(const LaunchCtx&, const Grid&, const Grid&, int, const T*, const T*,          \
+                                        const T*, const uint8_t*, T*, double, int, const T*, int, int);              \
+    template int launchJacobiZero<T>(const LaunchCtx&, const Grid&, const T*, const T*, const uint8_t*, T*, double,  \
+                                     int);                                                                           \
+    template int launchProlongAdd<T>(const LaunchCtx&, const Grid&, const Grid&, int, const T*, const uint8_t*, T*,  \
+                                     int);                                                                           \
+    template int launchCoarseSolve<T>(const LaunchCtx&, const T*, int64_t, const int32_t*, const T*, T*, T*, int);   \
+    template int launchUpdateP<T>(const LaunchCtx&, int64_t, T*, const T*, int);                                     \
+    template int launchDots<T>(const LaunchCtx&, int64_t, const T*, const T*, const T*, const T*, int, int);         \
+    template int launchFill<T>(cudaStream_t, int64_t, T*, T);                                                        \
+    template int launchScatterCompressed<T>(cudaStream_t, int64_t, const int32_t*, const double*, T*);               \
+    template int launchGatherCompressed<T>(cudaStream_t, int64_t, const int32_t*, const T*, double*);
+INST_T(double)
+INST_T(float)
+template int launchUpdateXR<double, double>(const LaunchCtx&, int64_t, double*, double*, const double*, const double*);
+template int launchUpdateXR<double, float>(const LaunchCtx&, int64_t, double*, float*, const float*, const float*);
+template int launchConvert<double, float>(cudaStream_t, int64_t, const double*, float*);
+template int launchConvert<float, double>(cudaStream_t, int64_t, const float*, double*);
+template int launchConvert<double, double>(cudaStream_t, int64_t, const double*, double*);
+template int launchConvert<float, float>(cudaStream_t, int64_t, const float*, float*);
+
+}  // namespace vfem

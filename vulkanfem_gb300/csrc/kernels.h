@@ -1,0 +1,153 @@
+// kernels.h -- launch interface of the sm_103a kernels (kernels.cu).
+//
+// All kernels run on one stream in a fixed order, so they share one
+// reduction buffer (block partials + ticket).  Solver scalars live in device
+// memory (Scalars) so that a whole PCG iteration runs without a host round
+// trip: each kernel returns immediately once `done` is set, and the host polls
+// `done` once per chunk of iterations.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "vfem_internal.h"
+
+namespace vfem {
+
+enum Done : int { RUNNING = 0, CONVERGED = 1, MAXITER = 2, BREAKDOWN = 3 };
+
+struct Scalars {
+    double rhsNorm2, threshold, tol2;
+    double rho, rhoOld, pAp, rr, alpha, beta, zAp, rrTrue;
+    double red0, red1;
+    long long iter, maxIter, matvecs, replacements;
+    int done;
+    int checkPending;  // mixed precision: recursive residual passed, verify in FP64
+    int flexible;
+    int mixed;
+    int replaceEvery;
+    int pad;
+};
+
+struct RedBuf {
+    double* partials;   // 2 * kMaxBlocks
+    unsigned* ticket;
+};
+
+constexpr int kMaxRedBlocks = 1 << 16;
+
+// What the last block of a reducing kernel does with the totals (t0, t1).
+enum Epi : int {
+    EPI_NONE = 0,
+    EPI_STORE = 1,   // red0 = t0, red1 = t1
+    EPI_ALPHA = 2,   // pAp = t0 -> alpha = rho / pAp
+    EPI_CONV = 3,    // rr = t0 -> convergence test
+    EPI_RHO0 = 4,    // rho = t0 (r.z of the first preconditioned residual)
+    EPI_BETA = 5,    // rho = t0, zAp = t1 -> beta, iteration count
+    EPI_INIT = 6,    // rhsNorm2 = t0, rr = t1 -> threshold
+    EPI_TRUE = 7     // rrTrue = t0 (FP64 residual) -> replacement / final check
+};
+
+// Matvec output modes.
+enum MvMode : int {
+    MV_AX = 0,       // y = A x (fixed rows zeroed)
+    MV_RESID = 1,    // y = f - A x
+    MV_RESID0 = 2,   // y = f - A x, zero at fixed nodes
+    MV_SMOOTH = 3    // y = x + omega D^-1 (f - A x), zero at fixed nodes
+};
+
+// Dot selections of a matvec / prolongation pass.
+enum DotSel : int { DOT_NONE = 0, DOT_X_OUT = 1, DOT_OUT_OUT = 2, DOT_F_OUT = 3 };
+
+template <typename T>
+struct MatvecArgs {
+    Grid g;
+    const float* E;
+    const uint8_t* flags;
+    const T* x;
+    T* y;
+    const T* f;        // MV_RESID*, MV_SMOOTH
+    const T* dinv;     // MV_SMOOTH
+    const T* aux;      // second dot: out . aux
+    float* y32;        // optional FP32 copy of y (mixed-precision residual replacement)
+    double scale;      // operator multiplier on this level
+    double omega;
+    int mode, dot0, dot1, epi;
+    int condTrue;      // run only when a true-residual pass is due (mixed precision)
+    int checkDone;
+};
+
+struct OpConst64 { double ks[45]; double ke[576]; };
+struct OpConst32 { float ks[45]; float ke[576]; };
+
+struct LaunchCtx {
+    cudaStream_t stream;
+    Scalars* S;
+    RedBuf rb;
+};
+
+// Opt the matvec kernels into > 48 KB of dynamic shared memory (once per device).
+cudaError_t setKernelAttributes();
+
+// ---- launchers (return the number of kernels launched) ----
+template <typename T>
+int launchMatvec(const LaunchCtx& c, const MatvecArgs<T>& a, bool structured, const void* opconst);
+
+template <typename T>
+int launchRestrict(const LaunchCtx& c, const Grid& gf, const Grid& gc, int div, const T* rf, T* rc,
+                   int checkDone);
+
+// Reference-mode up-leg: zf = used ? P zc + coef * dinv o rf : 0 (fixed -> 0 on level 0),
+// optional dots r.z and z.aux with epilogue `epi`.
+template <typename T>
+int launchProlongSmooth(const LaunchCtx& c, const Grid& gf, const Grid& gc, int div, const T* zc, const T* rf,
+                        const T* dinv, const uint8_t* flags, T* zf, double coef, int maskFixed,
+                        const T* aux, int epi, int checkDone);
+
+// V-cycle helpers: z = mask(omega dinv r); zf += mask(P zc).
+template <typename T>
+int launchJacobiZero(const LaunchCtx& c, const Grid& g, const T* r, const T* dinv, const uint8_t* flags, T* z,
+                     double omega, int checkDone);
+template <typename T>
+int launchProlongAdd(const LaunchCtx& c, const Grid& gf, const Grid& gc, int div, const T* zc,
+                     const uint8_t* flags, T* zf, int checkDone);
+
+// Coarsest level: zc[free] = Kinv * rc[free].
+template <typename T>
+int launchCoarseSolve(const LaunchCtx& c, const T* Kinv, int64_t n, const int32_t* freeDof, const T* rc, T* tmp,
+                      T* zc, int checkDone);
+
+// CG vector updates on flat arrays of length n.
+// x += alpha p ; r -= alpha Ap ; rr -> EPI_CONV
+template <typename TX, typename TV>
+int launchUpdateXR(const LaunchCtx& c, int64_t n, TX* x, TV* r, const TV* p, const TV* Ap);
+// p = z + beta p
+template <typename T>
+int launchUpdateP(const LaunchCtx& c, int64_t n, T* p, const T* z, int first);
+// sums (a.b, c.d) -> epi  (pointers may alias; null pair -> 0)
+template <typename T>
+int launchDots(const LaunchCtx& c, int64_t n, const T* a, const T* b, const T* cc, const T* d, int epi,
+               int checkDone);
+// y = x (with type conversion), optional x2 -> y2 zero fill
+template <typename TI, typename TO>
+int launchConvert(cudaStream_t s, int64_t n, const TI* x, TO* y);
+template <typename T>
+int launchFill(cudaStream_t s, int64_t n, T* y, T v);
+
+// compressed <-> dense storage
+template <typename T>
+int launchScatterCompressed(cudaStream_t s, int64_t nnodes, const int32_t* nodeStore, const double* comp, T* dense);
+template <typename T>
+int launchGatherCompressed(cudaStream_t s, int64_t nnodes, const int32_t* nodeStore, const T* dense, double* comp);
+
+// Coarsest-matrix assembly (dense, free DOFs only), one parity colour per launch.
+int launchAssembleCoarse(cudaStream_t s, const Grid& g, const float* E, const int32_t* freeNode, const double* Ke,
+                         double scale, double* K, int64_t n);
+int launchSymmetrizeLowerToFull(cudaStream_t s, double* K, int64_t n);
+
+// Solver scalar initialisation (device side, so it can live in a graph).
+int launchInitScalars(cudaStream_t s, Scalars* S, double tol, long long maxIter, int flexible, int mixed,
+                      int replaceEvery);
+
+// Device-side ``done`` / iteration snapshot is read back by the host with a plain copy.
+
+}  // namespace vfem
