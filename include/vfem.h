@@ -78,7 +78,9 @@ typedef struct vfem_options {
     int32_t check_every;     /* iterations per device-side chunk between host polls; default 8 */
     int32_t compute_true_residual; /* 1: report the true FP64 residual at exit (one extra FP64 product
                                       outside the timed solve for VFEM_PREC_FP64); default 1 */
-    int32_t reserved[7];
+    double replace_delta;    /* mixed precision: also replace the residual once |r| has dropped by this
+                                factor since the last replacement (reliable updates); default 0.1, 0 = off */
+    int32_t reserved[6];
 } vfem_options;
 
 typedef struct vfem_stats {
@@ -163,6 +165,30 @@ vfem_status vfem_inverse_diagonal(vfem_problem* p, int32_t level, double* out);
 /* Fixed nodes of `level` (fixedNodesInLevels, FEM.cpp:402-460): writes up to
  * `cap` compressed ids and the total count. */
 vfem_status vfem_fixed_nodes(vfem_problem* p, int32_t level, int64_t* out, int64_t cap, int64_t* count);
+
+/* Kernel classes timed by vfem_profile_kernels. */
+typedef enum vfem_kernel_class {
+    VFEM_K_MATVEC_FP64 = 0,
+    VFEM_K_MATVEC_FP32 = 1,
+    VFEM_K_RESTRICT_FP64 = 2,
+    VFEM_K_RESTRICT_FP32 = 3,
+    VFEM_K_PROLONG_FP64 = 4,
+    VFEM_K_PROLONG_FP32 = 5,
+    VFEM_K_UPDATE_XR_FP64 = 6,
+    VFEM_K_UPDATE_XR_MIXED = 7,
+    VFEM_K_UPDATE_P_FP64 = 8,
+    VFEM_K_UPDATE_P_FP32 = 9,
+    VFEM_K_COARSE_FP64 = 10,
+    VFEM_K_COARSE_FP32 = 11,
+    VFEM_K_COUNT = 12
+} vfem_kernel_class;
+
+/* Measurement helper (no counterpart in the reference): average device time in
+ * milliseconds of `reps` back-to-back launches of each kernel class on the finest
+ * level (transfers between levels 0 and 1; coarse = the coarsest dense solve),
+ * timed with CUDA events on the problem's stream.  ms_out has VFEM_K_COUNT
+ * entries.  Overwrites the problem's work vectors. */
+vfem_status vfem_profile_kernels(vfem_problem* p, int32_t reps, double* ms_out);
 
 /* Number of kernels this library has launched in this process (all problems). */
 int64_t vfem_kernel_launch_count(void);

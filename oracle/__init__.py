@@ -48,6 +48,9 @@ def _load():
         lib.oracle_create.restype = P
         lib.oracle_create.argtypes = [i32p, ctypes.c_int, ctypes.c_int, ctypes.c_int, f64p,
                                       i64p, ctypes.c_int64, ctypes.c_int, ctypes.c_int]
+        lib.oracle_create_e.restype = P
+        lib.oracle_create_e.argtypes = [i32p, ctypes.c_int, ctypes.c_int, ctypes.c_int, f64p, ctypes.c_void_p,
+                                        i64p, ctypes.c_int64, ctypes.c_int, ctypes.c_int]
         lib.oracle_destroy.argtypes = [P]
         lib.oracle_set_threads.argtypes = [P, ctypes.c_int]
         lib.oracle_set_float_coeffs.argtypes = [P, ctypes.c_int]
@@ -80,15 +83,21 @@ def _load():
 class Oracle:
     """One assembled problem (the reference's ``assembleSystemMatrix`` result)."""
 
-    def __init__(self, voxels, Ke, fixed, num_levels=3, skip_levels=0, threads=1):
+    def __init__(self, voxels, Ke, fixed, num_levels=3, skip_levels=0, threads=1, E=None):
         lib = _load()
         vox = np.ascontiguousarray(voxels, dtype=np.int32)
         assert vox.ndim == 3, "voxels are indexed [z, y, x]"
         sz, sy, sx = vox.shape
         ke = np.ascontiguousarray(Ke, dtype=np.float64).reshape(24, 24)
         fx = np.ascontiguousarray(fixed, dtype=np.int64).reshape(-1)
-        self._p = lib.oracle_create(vox.reshape(-1), sx, sy, sz, ke.reshape(-1), fx, fx.size,
-                                    int(num_levels), int(skip_levels))
+        self._E = None
+        eptr = None
+        if E is not None:  # per-voxel modulus (extension; the reference has a uniform E)
+            self._E = np.ascontiguousarray(E, dtype=np.float32)
+            assert self._E.shape == vox.shape
+            eptr = self._E.ctypes.data_as(ctypes.c_void_p)
+        self._p = lib.oracle_create_e(vox.reshape(-1), sx, sy, sz, ke.reshape(-1), eptr, fx, fx.size,
+                                      int(num_levels), int(skip_levels))
         if not self._p:
             raise ValueError("oracle_create failed")
         self._lib = lib

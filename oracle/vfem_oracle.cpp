@@ -59,6 +59,7 @@ inline double tri1(int a, int b, int div) {
 struct Level {
     int ex = 0, ey = 0, ez = 0;          // levelDims (FEM.cpp:246,256-260)
     std::vector<V3> elements;            // levelElements, sorted by linear index
+    std::vector<double> elemE;           // modulus multiplier per element (extension; 1 in the reference)
     std::vector<int64_t> nodes;          // used node linear ids in the node grid, sorted
     std::vector<int32_t> lookup;         // node grid linear id -> compressed id (or -1)
     std::vector<std::array<int, 4>> e2n; // elementToNode, 4 columns (FEM.cpp:188-198,332,345)
@@ -135,14 +136,17 @@ void childDiag(const double Ke[24][24], int div, std::vector<double>& tab) {
 
 // ---------------------------------------------------------------- assembly
 // EnlistUsedElements (FEM.cpp:66-100) + compressed numbering (FEM.cpp:179-186).
-void buildFinest(Problem& P, const int32_t* vox, int sx, int sy, int sz) {
+void buildFinest(Problem& P, const int32_t* vox, int sx, int sy, int sz, const float* E) {
     Level& l = P.L[0];
     l.ex = sx; l.ey = sy; l.ez = sz;
     int nx = sx + 1, ny = sy + 1, nz = sz + 1;
     for (int z = 0; z < sz; ++z)
         for (int y = 0; y < sy; ++y)
             for (int x = 0; x < sx; ++x)
-                if (vox[lin(x, y, z, sx, sy)] == 1) l.elements.push_back({x, y, z});
+                if (vox[lin(x, y, z, sx, sy)] == 1) {
+                    l.elements.push_back({x, y, z});
+                    l.elemE.push_back(E ? (double)E[lin(x, y, z, sx, sy)] : 1.0);
+                }
     l.lookup.assign((size_t)nx * ny * nz, -1);
     std::vector<uint8_t> used((size_t)nx * ny * nz, 0);
     for (auto& e : l.elements)
@@ -169,7 +173,7 @@ void inverseDiagonal(Level& l, double scale, const double Ke[24][24],
     for (size_t i = 0; i < l.e2n.size(); ++i) {
         for (int k = 0; k < 24; ++k) {
             int64_t dof = 3 * (int64_t)l.e2n[i][k / 6] + (k % 6);
-            double d = (unique && !(*unique)[i].empty()) ? (*unique)[i][k] : scale * Ke[k][k];
+            double d = (unique && !(*unique)[i].empty()) ? (*unique)[i][k] : scale * l.elemE[i] * Ke[k][k];
             diag[dof] += d;
         }
     }
@@ -200,19 +204,26 @@ void buildLevels(Problem& P, int numLevels) {
         // element grid used for linearisation has dims c.ex.. (levelDims[i]).
         int64_t ncell = (int64_t)c.ex * c.ey * c.ez;
         std::vector<int32_t> childCount(ncell, 0);
-        std::vector<uint8_t> childMask;  // per coarse cell, bitmask over children (div==2)
-        std::vector<std::vector<int>> childList(ncell);
-        for (auto& fe : f.elements) {
+        std::vector<std::vector<std::pair<int, double>>> childList(ncell);  // (child slot, modulus)
+        for (size_t fi = 0; fi < f.elements.size(); ++fi) {
+            const V3& fe = f.elements[fi];
             int x = fe.x / div, y = fe.y / div, z = fe.z / div;
             int64_t id = lin(x, y, z, c.ex, c.ey);
             int chx = fe.x - x * div, chy = fe.y - y * div, chz = fe.z - z * div;
-            childList[id].push_back(chx + div * (chy + div * chz));
+            childList[id].push_back({chx + div * (chy + div * chz), f.elemE[fi]});
             childCount[id]++;
         }
         for (int z = 0; z < c.ez; ++z)
             for (int y = 0; y < c.ey; ++y)
-                for (int x = 0; x < c.ex; ++x)
-                    if (childCount[lin(x, y, z, c.ex, c.ey)] > 0) c.elements.push_back({x, y, z});
+                for (int x = 0; x < c.ex; ++x) {
+                    int64_t id = lin(x, y, z, c.ex, c.ey);
+                    if (childCount[id] == 0) continue;
+                    c.elements.push_back({x, y, z});
+                    // Extension: a coarse element carries the mean modulus of its used children.
+                    double s = 0.0;
+                    for (auto& ch : childList[id]) s += ch.second;
+                    c.elemE.push_back((double)(float)(s / childCount[id]));
+                }
         // Coarse nodes and numbering (FEM.cpp:291-319).
         int cnx = c.nx(), cny = c.ny(), cnz = c.nz();
         std::vector<uint8_t> used((size_t)cnx * cny * cnz, 0);
@@ -254,8 +265,8 @@ void buildLevels(Problem& P, int numLevels) {
             int64_t cell = lin(e.x, e.y, e.z, c.ex, c.ey);
             if (childCount[cell] < nch) {
                 std::vector<double> d(24, 0.0);
-                for (int ch : childList[cell])
-                    for (int k = 0; k < 24; ++k) d[k] += childScale * tab[(size_t)ch * 24 + k];
+                for (auto& ch : childList[cell])
+                    for (int k = 0; k < 24; ++k) d[k] += childScale * ch.second * tab[(size_t)ch.first * 24 + k];
                 unique[ie] = d;
             }
         }
@@ -291,6 +302,7 @@ void restrictVec(const Problem& P, int lv, const double* r, double* out, bool us
     int div = c.divider, n = div + 1;
     std::fill(out, out + c.ndof(), 0.0);
     std::vector<double> tempR(f.ndof());
+#pragma omp parallel for num_threads(P.threads) schedule(static) if (P.threads > 1)
     for (int64_t k = 0; k < f.ndof(); ++k) {
         double w = useW ? f.W[k] : 1.0;
         if (P.floatCoeffs) w = (double)(float)w;
@@ -358,6 +370,7 @@ void interpolateVec(const Problem& P, int lv, const double* xc, double* out) {
     } else {
         for (size_t ie = 0; ie < c.elements.size(); ++ie) body(ie);
     }
+#pragma omp parallel for num_threads(P.threads) schedule(static) if (P.threads > 1)
     for (int64_t k = 0; k < f.ndof(); ++k) {
         double w = f.W[k];
         if (P.floatCoeffs) w = (double)(float)w;
@@ -404,7 +417,9 @@ void buildCoarse(Problem& P) {
     P.bw = bw;
     int64_t W = bw + 1;
     P.band.assign((size_t)N * W, 0.0);  // band[i*W + k] = A(i, i-k), k <= bw
-    for (auto& e : l.elements) {
+    for (size_t ie = 0; ie < l.elements.size(); ++ie) {
+        const V3& e = l.elements[ie];
+        const double me = mult * l.elemE[ie];
         for (int a = 0; a < 8; ++a) {
             int64_t ga = nodeOf(e, a);
             if (ga < 0) continue;
@@ -415,7 +430,7 @@ void buildCoarse(Problem& P) {
                     for (int c2 = 0; c2 < 3; ++c2) {
                         int64_t i = 3 * ga + c1, j = 3 * gb + c2;
                         if (j > i) continue;
-                        P.band[(size_t)i * W + (i - j)] += mult * P.Ke[3 * a + c1][3 * b + c2];
+                        P.band[(size_t)i * W + (i - j)] += me * P.Ke[3 * a + c1][3 * b + c2];
                     }
             }
         }
@@ -474,7 +489,7 @@ void matvec(const Problem& P, const double* x, double* y) {
         for (int r = 0; r < 24; ++r) {
             double s = 0.0;
             for (int k = 0; k < 24; ++k) s += P.Ke[r][k] * xe[k];
-            y[xs[r]] += s;
+            y[xs[r]] += l.elemE[i] * s;
         }
     };
     if (P.threads > 1) {
@@ -502,6 +517,7 @@ void precond(const Problem& P, const double* b, double* out) {
         return P.floatCoeffs ? (double)(float)v : v;
     };
     for (int i = 0; i < nl - 1; ++i) {
+#pragma omp parallel for num_threads(P.threads) schedule(static) if (P.threads > 1)
         for (int64_t k = 0; k < P.L[i].ndof(); ++k) xs[i][k] += rs[i][k] * dinv(i, k);  // smooth
         rs[i + 1].assign(P.L[i + 1].ndof(), 0.0);
         restrictVec(P, i, rs[i].data(), rs[i + 1].data());
@@ -516,7 +532,9 @@ void precond(const Problem& P, const double* b, double* out) {
     for (int i = nl - 1; i > 0; --i) {
         std::vector<double> t(P.L[i - 1].ndof());
         interpolateVec(P, i - 1, xs[i].data(), t.data());
+#pragma omp parallel for num_threads(P.threads) schedule(static) if (P.threads > 1)
         for (int64_t k = 0; k < P.L[i - 1].ndof(); ++k) xs[i - 1][k] += t[k];
+#pragma omp parallel for num_threads(P.threads) schedule(static) if (P.threads > 1)
         for (int64_t k = 0; k < P.L[i - 1].ndof(); ++k) xs[i - 1][k] += rs[i - 1][k] * dinv(i - 1, k);
     }
     std::copy(xs[0].begin(), xs[0].end(), out);
@@ -544,8 +562,11 @@ struct OracleProblem;
 // MULTIGRID definitions.  voxels: int32 occupancy (1 = filled), x fastest,
 // dims (sx, sy, sz).  Ke: 24x24 row-major; only its upper triangle is read
 // (FEM.cpp:200-210).  fixed: compressed node ids (0-based).
-OracleProblem* oracle_create(const int32_t* voxels, int sx, int sy, int sz, const double* Ke,
-                             const int64_t* fixed, int64_t nfixed, int numLevels, int skipLevels) {
+// Extension with no reference counterpart: E (per voxel, same layout as the
+// voxels, or null) multiplies the element stiffness; coarse elements carry the
+// mean modulus of their used children.  With E null the reference is unchanged.
+OracleProblem* oracle_create_e(const int32_t* voxels, int sx, int sy, int sz, const double* Ke, const float* E,
+                               const int64_t* fixed, int64_t nfixed, int numLevels, int skipLevels) {
     if (skipLevels < 0 || skipLevels > 1 || numLevels < 1) return nullptr;
     Problem* P = new Problem();
     P->skipLevels = skipLevels;
@@ -554,7 +575,7 @@ OracleProblem* oracle_create(const int32_t* voxels, int sx, int sy, int sz, cons
         for (int j = 0; j < i; ++j) P->Ke[i][j] = P->Ke[j][i] = Ke[j * 24 + i];
     }
     P->L.resize(1);
-    buildFinest(*P, voxels, sx, sy, sz);
+    buildFinest(*P, voxels, sx, sy, sz, E);
     std::vector<int64_t> fx(fixed, fixed + nfixed);
     std::sort(fx.begin(), fx.end());
     fx.erase(std::unique(fx.begin(), fx.end()), fx.end());
@@ -563,6 +584,11 @@ OracleProblem* oracle_create(const int32_t* voxels, int sx, int sy, int sz, cons
     buildLevels(*P, numLevels);
     buildCoarse(*P);
     return (OracleProblem*)P;
+}
+
+OracleProblem* oracle_create(const int32_t* voxels, int sx, int sy, int sz, const double* Ke,
+                             const int64_t* fixed, int64_t nfixed, int numLevels, int skipLevels) {
+    return oracle_create_e(voxels, sx, sy, sz, Ke, nullptr, fixed, nfixed, numLevels, skipLevels);
 }
 
 void oracle_destroy(OracleProblem* p) { delete (Problem*)p; }
@@ -643,7 +669,9 @@ int64_t oracle_pcg(OracleProblem* p, const double* b, double* x, double tol, int
     while (i < max_iter) {
         matvec(P, pv.data(), tmp.data());
         double alpha = absNew / dot(P, pv.data(), tmp.data(), n);
+#pragma omp parallel for num_threads(P.threads) schedule(static) if (P.threads > 1)
         for (int64_t k = 0; k < n; ++k) x[k] += alpha * pv[k];
+#pragma omp parallel for num_threads(P.threads) schedule(static) if (P.threads > 1)
         for (int64_t k = 0; k < n; ++k) r[k] -= alpha * tmp[k];
         resNorm2 = dot(P, r.data(), r.data(), n);
         if (resNorm2 < threshold) break;
@@ -652,6 +680,7 @@ int64_t oracle_pcg(OracleProblem* p, const double* b, double* x, double tol, int
         double absOld = absNew;
         absNew = dot(P, r.data(), z.data(), n);
         double beta = absNew / absOld;
+#pragma omp parallel for num_threads(P.threads) schedule(static) if (P.threads > 1)
         for (int64_t k = 0; k < n; ++k) pv[k] = z[k] + beta * pv[k];
         ++i;
     }

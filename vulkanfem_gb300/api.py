@@ -41,8 +41,12 @@ EXPORTED = (
     "vfem_problem_destroy", "vfem_problem_info", "vfem_problem_set_loads", "vfem_problem_set_rhs",
     "vfem_solve", "vfem_solve_device", "vfem_apply_operator", "vfem_apply_preconditioner",
     "vfem_restrict", "vfem_interpolate", "vfem_inverse_diagonal", "vfem_fixed_nodes",
-    "vfem_kernel_launch_count", "vfem_last_error_message",
+    "vfem_kernel_launch_count", "vfem_last_error_message", "vfem_profile_kernels",
 )
+
+KERNEL_CLASSES = ("matvec_fp64", "matvec_fp32", "restrict_fp64", "restrict_fp32", "prolong_fp64", "prolong_fp32",
+                  "update_xr_fp64", "update_xr_mixed", "update_p_fp64", "update_p_fp32", "coarse_fp64",
+                  "coarse_fp32")
 
 
 class VfemError(RuntimeError):
@@ -58,7 +62,7 @@ class Options(ctypes.Structure):
         ("precision", ctypes.c_int32), ("omega", ctypes.c_double), ("pre_sweeps", ctypes.c_int32),
         ("post_sweeps", ctypes.c_int32), ("replace_every", ctypes.c_int32), ("flexible", ctypes.c_int32),
         ("check_every", ctypes.c_int32), ("compute_true_residual", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 7),
+        ("replace_delta", ctypes.c_double), ("reserved", ctypes.c_int32 * 6),
     ]
 
 
@@ -117,6 +121,7 @@ def load_library(build_if_missing=True):
     lib.vfem_interpolate.argtypes = [P, i32, f64p, f64p]
     lib.vfem_inverse_diagonal.argtypes = [P, i32, f64p]
     lib.vfem_fixed_nodes.argtypes = [P, i32, ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)]
+    lib.vfem_profile_kernels.argtypes = [P, i32, f64p]
     for name in EXPORTED:
         fn = getattr(lib, name)
         if fn.restype is ctypes.c_int and name not in ("vfem_status_string",):
@@ -135,6 +140,13 @@ def kernel_launch_count():
     return int(load_library().vfem_kernel_launch_count())
 
 
+def profile_kernels(A, reps=20):
+    """Average CUDA-event time (ms) of each kernel class on A's finest level."""
+    out = np.zeros(len(KERNEL_CLASSES), np.float64)
+    _check(load_library().vfem_profile_kernels(A._h, int(reps), out))
+    return dict(zip(KERNEL_CLASSES, out.tolist()))
+
+
 def hex8_stiffness(E=1.0, nu=0.3):
     lib = load_library()
     ke = np.zeros(576, np.float64)
@@ -143,7 +155,8 @@ def hex8_stiffness(E=1.0, nu=0.3):
 
 
 def make_options(rtol=1e-6, max_iter=0, mg_mode="reference", precision="fp64", omega=0.6, pre_sweeps=1,
-                 post_sweeps=1, replace_every=50, flexible=False, check_every=8, compute_true_residual=True):
+                 post_sweeps=1, replace_every=50, flexible=False, check_every=8, compute_true_residual=True,
+                 replace_delta=0.1):
     lib = load_library()
     o = Options()
     lib.vfem_options_default(ctypes.byref(o))
@@ -158,6 +171,7 @@ def make_options(rtol=1e-6, max_iter=0, mg_mode="reference", precision="fp64", o
     o.flexible = int(bool(flexible))
     o.check_every = check_every
     o.compute_true_residual = int(bool(compute_true_residual))
+    o.replace_delta = replace_delta
     return o
 
 

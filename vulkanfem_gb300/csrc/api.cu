@@ -497,7 +497,7 @@ int iteration(vfem_problem* p, const vfem_options& o, double** zOut64, float** z
 vfem_status checkOptions(const vfem_options& o) {
     if (!(o.rtol > 0) || o.mg_mode < 0 || o.mg_mode > 2 || o.precision < 0 || o.precision > 1 ||
         (o.mg_mode == VFEM_MG_VCYCLE && (!(o.omega > 0) || o.pre_sweeps < 1 || o.post_sweeps < 0)) ||
-        o.check_every < 1 || o.check_every > 1024 || o.replace_every < 0)
+        o.check_every < 1 || o.check_every > 1024 || o.replace_every < 0 || !(o.replace_delta >= 0.0 && o.replace_delta < 1.0))
         return fail(VFEM_ERR_INVALID_ARGUMENT, "invalid solver options");
     return VFEM_OK;
 }
@@ -520,7 +520,7 @@ vfem_status solveImpl(vfem_problem* p, const vfem_options* optIn, bool haveX0, v
     CK(cudaEventCreate(&e1));
     CK(cudaEventRecord(e0, p->stream));
     launches += launchInitScalars(p->stream, p->S, o.rtol, maxIter, o.flexible, mixed ? 1 : 0,
-                                  mixed ? o.replace_every : 0);
+                                  mixed ? o.replace_every : 0, o.replace_delta);
     // ---- initial residual, norms, first direction
     double* z64 = nullptr;
     float* z32 = nullptr;
@@ -658,6 +658,7 @@ void vfem_options_default(vfem_options* o) {
     o->flexible = 0;
     o->check_every = 8;
     o->compute_true_residual = 1;
+    o->replace_delta = 0.1;
 }
 
 const char* vfem_status_string(vfem_status s) {
@@ -782,7 +783,7 @@ vfem_status vfem_apply_preconditioner(vfem_problem* p, int32_t mg_mode, const do
     vfem_options o;
     vfem_options_default(&o);
     o.mg_mode = mg_mode;
-    launchInitScalars(p->stream, p->S, 1e-6, 1, 0, 0, 0);
+    launchInitScalars(p->stream, p->S, 1e-6, 1, 0, 0, 0, 0.0);
     double* zo = nullptr;
     int k = 1 + vcycle<double>(p, o, 0, l0.r64, l0.z64, &zo, nullptr, EPI_NONE);
     p->launches += k;
@@ -799,7 +800,7 @@ vfem_status vfem_restrict(vfem_problem* p, int32_t level, const double* fine, do
     DevLevel& lc = p->L[level + 1];
     vfem_status s = toDenseHost(p, level, fine, lf.t64, nullptr);
     if (s != VFEM_OK) return s;
-    launchInitScalars(p->stream, p->S, 1e-6, 1, 0, 0, 0);
+    launchInitScalars(p->stream, p->S, 1e-6, 1, 0, 0, 0, 0.0);
     int k = 1 + launchRestrict<double>(ctx(p), lf.g, lc.g, lc.div, lf.t64, lc.t64, 0);
     p->launches += k;
     g_launches += k;
@@ -815,7 +816,7 @@ vfem_status vfem_interpolate(vfem_problem* p, int32_t level, const double* coars
     DevLevel& lc = p->L[level + 1];
     vfem_status s = toDenseHost(p, level + 1, coarse, lc.t64, nullptr);
     if (s != VFEM_OK) return s;
-    launchInitScalars(p->stream, p->S, 1e-6, 1, 0, 0, 0);
+    launchInitScalars(p->stream, p->S, 1e-6, 1, 0, 0, 0, 0.0);
     CK(cudaMemsetAsync(lf.t64, 0, sizeof(double) * (size_t)lf.nvec(), p->stream));
     // Masked trilinear prolongation only: coefficient 0 on the Jacobi term, no fixed mask
     // (the reference's interpolate does not zero fixed nodes).
@@ -825,6 +826,84 @@ vfem_status vfem_interpolate(vfem_problem* p, int32_t level, const double* coars
     g_launches += k;
     CK(cudaGetLastError());
     return fromDenseHost(p, level, lf.z64, fine);
+}
+
+vfem_status vfem_profile_kernels(vfem_problem* p, int32_t reps, double* ms) {
+    if (!p || !ms || reps < 1) return fail(VFEM_ERR_INVALID_ARGUMENT, "bad argument");
+    CK(cudaSetDevice(p->device));
+    DevLevel& l0 = p->L[0];
+    const bool two = p->L.size() > 1;
+    DevLevel& l1 = p->L[two ? 1 : 0];
+    const int64_t n = l0.nvec();
+    LaunchCtx c = ctx(p);
+    // Scalars with alpha = beta = 0 and done = 0: every kernel runs in full, vectors stay put.
+    launchInitScalars(p->stream, p->S, 1e-6, 1 << 30, 0, 0, 0, 0.0);
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    long long launched = 1;
+    for (int k = 0; k < VFEM_K_COUNT; ++k) {
+        auto one = [&]() -> int {
+            switch (k) {
+                case VFEM_K_MATVEC_FP64: {
+                    MatvecArgs<double> a = mvArgs<double>(p, 0, p->p64, p->Ap64, MV_AX);
+                    a.dot0 = DOT_X_OUT;
+                    a.epi = EPI_STORE;
+                    return matvec<double>(p, a);
+                }
+                case VFEM_K_MATVEC_FP32: {
+                    MatvecArgs<float> a = mvArgs<float>(p, 0, p->p32, p->Ap32, MV_AX);
+                    a.dot0 = DOT_X_OUT;
+                    a.epi = EPI_STORE;
+                    return matvec<float>(p, a);
+                }
+                case VFEM_K_RESTRICT_FP64:
+                    return two ? launchRestrict<double>(c, l0.g, l1.g, l1.div, l0.r64, l1.r64, 1) : 0;
+                case VFEM_K_RESTRICT_FP32:
+                    return two ? launchRestrict<float>(c, l0.g, l1.g, l1.div, l0.r32, l1.r32, 1) : 0;
+                case VFEM_K_PROLONG_FP64:
+                    return two ? launchProlongSmooth<double>(c, l0.g, l1.g, l1.div, l1.z64, l0.r64, l0.dinv64, l0.flags,
+                                                             l0.z64, 2.0, 1, nullptr, EPI_STORE, 1)
+                               : 0;
+                case VFEM_K_PROLONG_FP32:
+                    return two ? launchProlongSmooth<float>(c, l0.g, l1.g, l1.div, l1.z32, l0.r32, l0.dinv32, l0.flags,
+                                                            l0.z32, 2.0, 1, nullptr, EPI_STORE, 1)
+                               : 0;
+                case VFEM_K_UPDATE_XR_FP64:
+                    return launchUpdateXR<double, double>(c, n, p->x64, l0.r64, p->p64, p->Ap64);
+                case VFEM_K_UPDATE_XR_MIXED:
+                    return launchUpdateXR<double, float>(c, n, p->x64, l0.r32, p->p32, p->Ap32);
+                case VFEM_K_UPDATE_P_FP64:
+                    return launchUpdateP<double>(c, n, p->p64, l0.z64, 0);
+                case VFEM_K_UPDATE_P_FP32:
+                    return launchUpdateP<float>(c, n, p->p32, l0.z32, 0);
+                case VFEM_K_COARSE_FP64: {
+                    DevLevel& lc = p->L.back();
+                    return launchCoarseSolve<double>(c, p->Kinv64, p->nc, p->freeDof, lc.r64, p->cb64, lc.z64, 1);
+                }
+                default: {
+                    DevLevel& lc = p->L.back();
+                    return launchCoarseSolve<float>(c, p->Kinv32, p->nc, p->freeDof, lc.r32, p->cb32, lc.z32, 1);
+                }
+            }
+        };
+        launched += one() + one();
+        CK(cudaEventRecord(e0, p->stream));
+        int cnt = 0;
+        for (int r = 0; r < reps; ++r) cnt += one();
+        CK(cudaEventRecord(e1, p->stream));
+        CK(cudaEventSynchronize(e1));
+        launched += cnt;
+        float t = 0;
+        cudaEventElapsedTime(&t, e0, e1);
+        ms[k] = cnt ? (double)t / reps : 0.0;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    p->launches += launched;
+    g_launches += launched;
+    CK(cudaGetLastError());
+    return VFEM_OK;
 }
 
 vfem_status vfem_inverse_diagonal(vfem_problem* p, int32_t level, double* out) {

@@ -120,12 +120,14 @@ __device__ void applyEpi(int epi, Scalars* S, double t0, double t1) {
         case EPI_INIT:
             S->rhsNorm2 = t0;
             S->rr = t1;
+            S->rrLast = t1;
             S->threshold = fmax(S->tol2 * t0, DBL_MIN);
             if (t0 == 0.0 || t1 < S->threshold) S->done = CONVERGED;
             break;
         case EPI_TRUE:
             S->rrTrue = t0;
             S->rr = t0;
+            S->rrLast = t0;
             S->checkPending = 0;
             S->replacements++;
             if (!isfinite(t0)) S->done = BREAKDOWN;
@@ -136,8 +138,14 @@ __device__ void applyEpi(int epi, Scalars* S, double t0, double t1) {
     }
 }
 
+// Mixed precision: the FP64 true residual replaces the FP32 recursive one when
+// the recursive residual claims convergence, every replaceEvery iterations, and
+// whenever it has dropped by delta since the last replacement (the reliable-
+// update rule of Sleijpen & van der Vorst, which keeps the FP32 drift small
+// relative to the residual being replaced).
 __device__ __forceinline__ bool trueResidualDue(const Scalars* S) {
-    return S->checkPending || (S->replaceEvery > 0 && S->iter > 0 && (S->iter % S->replaceEvery) == 0);
+    return S->checkPending || (S->replaceEvery > 0 && S->iter > 0 && (S->iter % S->replaceEvery) == 0) ||
+           (S->delta2 > 0.0 && S->rr < S->delta2 * S->rrLast);
 }
 
 template <typename T>
@@ -268,6 +276,11 @@ __global__ void __launch_bounds__(MV_TX* MV_TY)
     for (int k = z0 - 1; k < zend; ++k) {
         load(k + 1);
         __syncthreads();
+        // x at the owned node of layer k, read now: the next iteration's load
+        // overwrites this layer's buffer without waiting for the output phase.
+        T xo[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) xo[c] = SU(k & 1, ty + 1, tx + 1, c);
         T ye[24];
         float Ee = 0.f;
         if (ecxy && k >= 0 && k < g.ez) Ee = a.E[g.store(ecx, ecy, k)];
@@ -307,14 +320,13 @@ __global__ void __launch_bounds__(MV_TX* MV_TY)
                 const int64_t s = g.store(onx, ony, k);
                 const uint8_t fl = a.flags[s];
                 const bool fixed = (fl & FLAG_FIXED) != 0;
-                const int b = k & 1;
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
                     const T ax = fixed ? T(0) : acc[c] + lo[c];
                     T out;
                     T fv = T(0);
                     if (a.mode != MV_AX) fv = a.f[3 * s + c];
-                    const T xv = SU(b, ty + 1, tx + 1, c);
+                    const T xv = xo[c];
                     switch (a.mode) {
                         case MV_AX: out = ax; break;
                         case MV_RESID: out = fv - ax; break;
@@ -622,13 +634,15 @@ __global__ void kSymmetrize(double* K, int64_t n) {
     }
 }
 
-__global__ void kInitScalars(Scalars* S, double tol, long long maxIter, int flexible, int mixed, int replaceEvery) {
+__global__ void kInitScalars(Scalars* S, double tol, long long maxIter, int flexible, int mixed, int replaceEvery,
+                             double delta) {
     Scalars s = {};
     s.tol2 = tol * tol;
     s.maxIter = maxIter;
     s.flexible = flexible;
     s.mixed = mixed;
     s.replaceEvery = replaceEvery;
+    s.delta2 = mixed ? delta * delta : 0.0;
     *S = s;
 }
 
@@ -787,8 +801,8 @@ int launchSymmetrizeLowerToFull(cudaStream_t s, double* K, int64_t n) {
 }
 
 int launchInitScalars(cudaStream_t s, Scalars* S, double tol, long long maxIter, int flexible, int mixed,
-                      int replaceEvery) {
-    kInitScalars<<<1, 1, 0, s>>>(S, tol, maxIter, flexible, mixed, replaceEvery);
+                      int replaceEvery, double replaceDelta) {
+    kInitScalars<<<1, 1, 0, s>>>(S, tol, maxIter, flexible, mixed, replaceEvery, replaceDelta);
     return 1;
 }
 

@@ -19,6 +19,8 @@ struct Scalars {
     double rhsNorm2, threshold, tol2;
     double rho, rhoOld, pAp, rr, alpha, beta, zAp, rrTrue;
     double red0, red1;
+    double rrLast;     // r.r at the last true-residual replacement (mixed precision)
+    double delta2;     // replace when r.r < delta2 * rrLast (reliable-update criterion)
     long long iter, maxIter, matvecs, replacements;
     int done;
     int checkPending;  // mixed precision: recursive residual passed, verify in FP64
@@ -146,7 +148,7 @@ int launchSymmetrizeLowerToFull(cudaStream_t s, double* K, int64_t n);
 
 // Solver scalar initialisation (device side, so it can live in a graph).
 int launchInitScalars(cudaStream_t s, Scalars* S, double tol, long long maxIter, int flexible, int mixed,
-                      int replaceEvery);
+                      int replaceEvery, double replaceDelta);
 
 // Device-side ``done`` / iteration snapshot is read back by the host with a plain copy.
 
