@@ -7,7 +7,7 @@
  *   assembleSystemMatrix<double>(...)      include/FEM.hpp:33-34, src/FEM.cpp:157-554
  *   applyBoundaryConditions(f, loads, ...) include/FEM.hpp:63-64, src/FEM.cpp:568-584
  *   solveWithKompute(A, f, u)              include/FEMGPU.hpp:11-12, src/FEMGPU.cpp:32-554
- *   solveWithEigen(A, f, u)                include/FEM.hpp:78-79,   src/FEM.cpp:589-637
+ *   solveWithEigen(A, f, u)                include/FEM.hpp:72-73,   src/FEM.cpp:589-637
  *   MatrixFreeSparse<double> * x           include/MatrixFreeSparse.hpp:31-94,191-215
  *   MultigridPreconditioner::solve(b)      include/MultigridPreconditioner.hpp:24-203
  *   MultigridPreconditioner::restrict / interpolate

@@ -43,6 +43,19 @@ def test_host_helpers_without_gpu():
     assert lib.vfem_hex8_stiffness(1.0, 0.5, bad) == 1  # nu = 0.5 is invalid
 
 
+def test_cpp_shim_compiles_and_links(tmp_path):
+    """include/vfem.hpp (reference names over the C ABI) builds a reference-style caller."""
+    import subprocess
+    from vulkanfem_gb300 import build as vbuild
+    lib = api.load_library() and vbuild.LIB
+    exe = tmp_path / "shim_example"
+    cmd = ["g++", "-std=c++17", "-I", os.path.join(ROOT, "include"), os.path.join(ROOT, "tests", "shim_example.cpp"),
+           lib, "-Wl,-rpath," + os.path.dirname(lib), "-o", str(exe)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert exe.exists()
+
+
 def test_create_reports_errors_instead_of_aborting():
     """Invalid input returns a status code (the reference asserts or misbehaves)."""
     lib = api.load_library()
