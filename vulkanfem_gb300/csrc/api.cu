@@ -237,6 +237,19 @@ vfem_status createImpl(const uint8_t* vox, int nx, int ny, int nz, const double*
         delete p;
         return fail(st, "Ke has non-finite entries");
     }
+    {
+        // Reducing kernels keep one partial per block; the largest grids are the
+        // matvec tiles (31 x 7 x 16 owned nodes) and the 32 x 8 x 8-node per-node kernels.
+        const int64_t gx = nx + 1, gy = ny + 1, gz = nz + 1;
+        const int64_t mv = ((gx + 30) / 31) * ((gy + 6) / 7) * ((gz + 15) / 16);
+        const int64_t pn = ((gx + 31) / 32) * ((gy + 7) / 8) * ((gz + 7) / 8);
+        if (mv > kMaxRedBlocks || pn > kMaxRedBlocks) {
+            delete p;
+            return fail(VFEM_ERR_INVALID_ARGUMENT, "grid too large for the reduction buffer (" +
+                                                       std::to_string(std::max(mv, pn)) + " blocks > " +
+                                                       std::to_string(kMaxRedBlocks) + ")");
+        }
+    }
     std::string err;
     st = buildHierarchy(vox, nx, ny, nz, E, fixed, nfixed, numLevels, skip, p->ke, p->H, err);
     if (st != VFEM_OK) {
