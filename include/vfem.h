@@ -148,6 +148,30 @@ vfem_status vfem_solve_device(vfem_problem* p, const vfem_options* opt, double* 
  * fixed rows zeroed. */
 vfem_status vfem_apply_operator(vfem_problem* p, const double* x, double* y);
 
+/* No counterpart in the reference.  The operator product of vfem_apply_operator
+ * for callers that cannot allocate GPU memory at the point of the call: code
+ * running while a stream is captured into a CUDA graph (cudaMalloc is not
+ * allowed there), hosts that hand every byte of device memory to their own pool
+ * up front, and loops that must not stall on cudaMalloc's implicit device
+ * synchronisation.  It calls no cudaMalloc, cudaFree or allocating library
+ * routine.  The caller passes device arrays: x_device and y_device hold 3
+ * doubles per node of the full node grid, (nx+1)*(ny+1)*(nz+1) nodes, x
+ * fastest (the grid index replaces the compressed node id; values of x at
+ * unused nodes are ignored, and y is written at every grid node, 0 at unused
+ * nodes and fixed rows), and xKx_device receives
+ * x.(Kx) in FP64.  Work is enqueued on `stream` (a cudaStream_t; NULL = the
+ * default stream); the call returns without synchronising.
+ * Scratch: a fixed 1,049,600-byte device array inside the library (reduction
+ * partials for up to 65,536 blocks of the product, i.e. node grids up to about
+ * 600^3); larger grids are rejected with VFEM_ERR_INVALID_ARGUMENT.  Every GPU
+ * that loads the library holds the array until the process exits.  All calls
+ * share it and it keeps the last call's contents; each call clears what must
+ * start at zero, but calls that overlap on the GPU race.  The first call on a
+ * device looks up the array's device address: make that first call before any
+ * stream capture. */
+vfem_status vfem_apply_operator_device_noalloc(vfem_problem* p, const double* x_device, double* y_device,
+                                               double* xKx_device, void* stream);
+
 /* MultigridPreconditioner::solve (MultigridPreconditioner.hpp:158-193): one
  * V-cycle of `mg_mode` (VFEM_MG_REFERENCE or VFEM_MG_VCYCLE) in FP64. */
 vfem_status vfem_apply_preconditioner(vfem_problem* p, int32_t mg_mode, const double* r, double* z);

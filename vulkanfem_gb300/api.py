@@ -42,6 +42,7 @@ EXPORTED = (
     "vfem_solve", "vfem_solve_device", "vfem_apply_operator", "vfem_apply_preconditioner",
     "vfem_restrict", "vfem_interpolate", "vfem_inverse_diagonal", "vfem_fixed_nodes",
     "vfem_kernel_launch_count", "vfem_last_error_message", "vfem_profile_kernels",
+    "vfem_apply_operator_device_noalloc",
 )
 
 KERNEL_CLASSES = ("matvec_fp64", "matvec_fp32", "restrict_fp64", "restrict_fp32", "prolong_fp64", "prolong_fp32",
@@ -122,6 +123,8 @@ def load_library(build_if_missing=True):
     lib.vfem_inverse_diagonal.argtypes = [P, i32, f64p]
     lib.vfem_fixed_nodes.argtypes = [P, i32, ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)]
     lib.vfem_profile_kernels.argtypes = [P, i32, f64p]
+    lib.vfem_apply_operator_device_noalloc.argtypes = [P, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                                       ctypes.c_void_p]
     for name in EXPORTED:
         fn = getattr(lib, name)
         if fn.restype is ctypes.c_int and name not in ("vfem_status_string",):

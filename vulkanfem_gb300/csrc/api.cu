@@ -786,6 +786,21 @@ vfem_status vfem_apply_operator(vfem_problem* p, const double* x, double* y) {
     return fromDenseHost(p, 0, p->Ap64, y);
 }
 
+vfem_status vfem_apply_operator_device_noalloc(vfem_problem* p, const double* x_device, double* y_device,
+                                               double* xKx_device, void* stream) {
+    if (!p || !x_device || !y_device || !xKx_device) return fail(VFEM_ERR_INVALID_ARGUMENT, "null argument");
+    CK(cudaSetDevice(p->device));  // the scratch set-up below runs with the problem's device current
+    MatvecArgs<double> a = mvArgs<double>(p, 0, x_device, y_device, MV_AX);
+    bool tooLarge = false;
+    CK(launchMatvecNoAlloc(static_cast<cudaStream_t>(stream), a, p->ke.structured, p->op64, xKx_device, &tooLarge));
+    if (tooLarge)
+        return fail(VFEM_ERR_INVALID_ARGUMENT,
+                    "grid too large for the no-allocation scratch (at most 65536 product blocks of 31x7x16 nodes)");
+    p->launches += 1;
+    g_launches += 1;
+    return VFEM_OK;
+}
+
 vfem_status vfem_apply_preconditioner(vfem_problem* p, int32_t mg_mode, const double* r, double* z) {
     if (!p || !r || !z || (mg_mode != VFEM_MG_REFERENCE && mg_mode != VFEM_MG_VCYCLE))
         return fail(VFEM_ERR_INVALID_ARGUMENT, "bad argument");

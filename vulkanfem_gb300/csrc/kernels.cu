@@ -17,6 +17,7 @@
 // fixed order by the last block to finish (no floating-point atomics).
 #include <cfloat>
 #include <cstdio>
+#include <mutex>
 
 #include "kernels.h"
 
@@ -804,6 +805,75 @@ int launchInitScalars(cudaStream_t s, Scalars* S, double tol, long long maxIter,
                       int replaceEvery, double replaceDelta) {
     kInitScalars<<<1, 1, 0, s>>>(S, tol, maxIter, flexible, mixed, replaceEvery, replaceDelta);
     return 1;
+}
+
+// ------------------------------------------------------------------ no-allocation product
+//
+// Scratch of vfem_apply_operator_device_noalloc: the reduction partials, the
+// ticket and the scalar block of the fused x.(Kx) dot live in this file-scope
+// device array instead of memory from cudaMalloc.  Fixed size: 2 x 65,536 block
+// partials + 1 KiB (1,049,600 bytes); every GPU that loads the library holds it
+// until the process exits.  All calls share it, so calls that overlap on the GPU
+// race; each call clears the ticket and scalars before its kernel.
+namespace {
+constexpr size_t kNoAllocPartialBytes = 2 * (size_t)kMaxRedBlocks * sizeof(double);
+constexpr size_t kNoAllocBytes = kNoAllocPartialBytes + 1024;
+static_assert(sizeof(Scalars) + 256 <= 1024, "scalar block does not fit the no-allocation scratch");
+__device__ __align__(256) unsigned char g_noallocScratch[kNoAllocBytes];
+std::mutex g_noallocMutex;
+constexpr int kNoAllocMaxDevices = 64;
+void* g_noallocAddr[kNoAllocMaxDevices] = {};
+}  // namespace
+
+cudaError_t noallocScratchSetup() {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_noallocMutex);
+    if (g_noallocAddr[dev]) return cudaSuccess;
+    void* ptr = nullptr;
+    e = cudaGetSymbolAddress(&ptr, g_noallocScratch);  // the host-side name is not a device address
+    if (e != cudaSuccess) return e;
+    g_noallocAddr[dev] = ptr;
+    return cudaSuccess;
+}
+
+cudaError_t launchMatvecNoAlloc(cudaStream_t s, const MatvecArgs<double>& a, bool structured, const void* opconst,
+                                double* xKx, bool* tooLarge) {
+    const Grid& g = a.g;
+    dim3 grid((g.nx + MV_TX - 2) / (MV_TX - 1), (g.ny + MV_TY - 2) / (MV_TY - 1), (g.nz + MV_ZC - 1) / MV_ZC);
+    *tooLarge = (int64_t)grid.x * grid.y * grid.z > kMaxRedBlocks;
+    if (*tooLarge) return cudaSuccess;
+    cudaError_t e = noallocScratchSetup();
+    if (e != cudaSuccess) return e;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    unsigned char* base = static_cast<unsigned char*>(g_noallocAddr[dev]);
+    RedBuf rb{reinterpret_cast<double*>(base), reinterpret_cast<unsigned*>(base + kNoAllocPartialBytes)};
+    Scalars* S = reinterpret_cast<Scalars*>(base + kNoAllocPartialBytes + 256);
+    // The ticket and the scalars must start at zero; the partials are overwritten.
+    if ((e = cudaMemsetAsync(base + kNoAllocPartialBytes, 0, 1024, s)) != cudaSuccess) return e;
+    MatvecArgs<double> b = a;
+    b.mode = MV_AX;
+    b.dot0 = DOT_X_OUT;
+    b.dot1 = 0;
+    b.epi = EPI_STORE;
+    b.checkDone = 0;
+    b.condTrue = 0;
+    size_t smem = (size_t)(kSuElems + kSyElems) * sizeof(double);
+    dim3 block(MV_TX, MV_TY);
+    if (structured) {
+        Ks<double> k;
+        for (int i = 0; i < 45; ++i) k.v[i] = static_cast<const double*>(opconst)[i];
+        kMatvec<double, true><<<grid, block, smem, s>>>(b, k, S, rb);
+    } else {
+        Kd<double> k;
+        for (int i = 0; i < 576; ++i) k.v[i] = static_cast<const double*>(opconst)[45 + i];
+        kMatvec<double, false><<<grid, block, smem, s>>>(b, k, S, rb);
+    }
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    return cudaMemcpyAsync(xKx, &S->red0, sizeof(double), cudaMemcpyDeviceToDevice, s);
 }
 
 // ------------------------------------------------------------------ instantiations

@@ -150,6 +150,14 @@ int launchSymmetrizeLowerToFull(cudaStream_t s, double* K, int64_t n);
 int launchInitScalars(cudaStream_t s, Scalars* S, double tol, long long maxIter, int flexible, int mixed,
                       int replaceEvery, double replaceDelta);
 
+// FP64 product y = K x with the fused x.(Kx) dot, its reduction scratch taken from
+// a file-scope device array (kernels.cu) instead of allocated memory.  The first
+// call on a device looks up that array's device address.  *tooLarge is set (and
+// nothing launched) when the product's grid needs more reduction blocks than
+// the array holds.  xKx is a device pointer.
+cudaError_t launchMatvecNoAlloc(cudaStream_t s, const MatvecArgs<double>& a, bool structured, const void* opconst,
+                                double* xKx, bool* tooLarge);
+
 // Device-side ``done`` / iteration snapshot is read back by the host with a plain copy.
 
 }  // namespace vfem
