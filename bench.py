@@ -37,6 +37,11 @@ WORKLOADS = {
                                                                                           lognormal_sigma=0.5),
                    "256^3 box minus 300 seeded spherical voids (r ~ U[4,16]), E ~ lognormal(0,0.5) per voxel, "
                    "nu=0.3, z=0 fixed, unit -z load on the top face, 5 MG levels"),
+    "spheres224": (lambda: __import__("vulkanfem_gb300.domains", fromlist=["x"]).spheres(224, 200, 4, 14, seed=0,
+                                                                                          levels=5,
+                                                                                          lognormal_sigma=0.5),
+                   "224^3 box minus 200 seeded spherical voids (r ~ U[4,14]), E ~ lognormal(0,0.5), 5 MG levels "
+                   "(smaller profiling case: FP32 vectors still exceed L2)"),
     "porous128": (lambda: __import__("vulkanfem_gb300.domains", fromlist=["x"]).porous(128, 0.40, 6.0, seed=0,
                                                                                         levels=4),
                   "128^3 seeded Gaussian random field (sigma 6 voxels) at 40% fill, grounded component, "
@@ -299,7 +304,7 @@ def main():
 
     # ---- comparison solver (plain FP64 MG-PCG on the same GPU)
     comp = None
-    if args.compare and args.compare != args.solver:
+    if args.compare and args.compare not in ("none", args.solver):
         copts = SOLVERS[args.compare]
         A.solve_device(**copts)
         cst = [A.solve_device(**copts)[1] for _ in range(max(1, args.compare_steps))]

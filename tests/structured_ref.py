@@ -110,3 +110,80 @@ def fixed_dilate(fine_fixed, coarse_shape, div=2):
                 vz, vy, vx = (Z >= 0) & (Z < fz), (Y >= 0) & (Y < fy), (X >= 0) & (X < fx)
                 out[np.ix_(vz, vy, vx)] |= fine_fixed[np.ix_(Z[vz], Y[vy], X[vx])]
     return out
+
+
+class MultiplicativeMG:
+    """numpy restatement of the library's multiplicative V-cycle
+    (VFEM_MG_VCYCLE): rediscretised level operators 2^l sum_e E_e Ke (coarse
+    elements carry the mean modulus of their used children), damped Jacobi on
+    their diagonals, full weighting / trilinear prolongation, fixed DOFs masked
+    on every level (fixed sets dilated from the finest), dense coarsest solve."""
+
+    def __init__(self, voxels, Ke, fixed, levels, E=None, omega=0.6, pre=1, post=1):
+        self.Ke, self.omega, self.pre, self.post = Ke, omega, pre, post
+        E0 = voxels.astype(float) * (np.asarray(E, np.float32).astype(float) if E is not None else 1.0)
+        self.Es, self.masks, self.fixeds, self.scales = [E0], [used_mask(E0 > 0)], [], [1.0]
+        fm = np.zeros(self.masks[0].shape, bool)
+        fm.reshape(-1)[np.flatnonzero(self.masks[0].reshape(-1))[np.asarray(fixed)]] = True
+        self.fixeds.append(fm)
+        for l in range(1, levels):
+            Ef = self.Es[-1]
+            ez, ey, ex = Ef.shape
+            cz, cy, cx = -(-ez // 2), -(-ey // 2), -(-ex // 2)
+            pad = np.zeros((cz * 2, cy * 2, cx * 2))
+            pad[:ez, :ey, :ex] = Ef
+            blk = pad.reshape(cz, 2, cy, 2, cx, 2)
+            cnt = (blk > 0).sum(axis=(1, 3, 5))
+            sm = blk.sum(axis=(1, 3, 5))
+            Ec = np.where(cnt > 0, (sm / np.maximum(cnt, 1)).astype(np.float32).astype(float), 0.0)
+            self.Es.append(Ec)
+            self.masks.append(used_mask(Ec > 0))
+            self.fixeds.append(fixed_dilate(self.fixeds[-1], self.masks[-1].shape, 2))
+            self.scales.append(2.0 ** l)
+        self.L = levels
+        self.act = [(m & ~f)[..., None] for m, f in zip(self.masks, self.fixeds)]
+        self.D = [self._dinv(l) for l in range(levels)]
+        lc = levels - 1
+        self.cidx = np.flatnonzero(self.act[lc][..., 0].reshape(-1))
+        n = 3 * self.cidx.size
+        Kc = np.zeros((n, n))
+        for j in range(n):
+            e = np.zeros(self.masks[lc].shape + (3,))
+            e.reshape(-1, 3)[self.cidx[j // 3], j % 3] = 1
+            Kc[:, j] = self.A(lc, e).reshape(-1, 3)[self.cidx].reshape(-1)
+        self.Kinv = np.linalg.inv(Kc)
+
+    def A(self, l, x):
+        return matvec(self.Es[l], self.Ke, x, self.fixeds[l], self.scales[l])
+
+    def _dinv(self, l):
+        diag = np.zeros(self.masks[l].shape + (3,))
+        Ee = self.Es[l]
+        ez, ey, ex = Ee.shape
+        for a in range(8):
+            dz, dy, dx = a >> 2, (a >> 1) & 1, a & 1
+            diag[dz:dz + ez, dy:dy + ey, dx:dx + ex] += self.scales[l] * Ee[..., None] * np.diag(self.Ke)[3 * a:3 * a + 3]
+        return np.where(self.masks[l][..., None], 1.0 / np.where(diag > 0, diag, 1.0), 0.0)
+
+    def _coarse(self, r):
+        z = np.zeros_like(r)
+        z.reshape(-1, 3)[self.cidx] = (self.Kinv @ r.reshape(-1, 3)[self.cidx].reshape(-1)).reshape(-1, 3)
+        return z
+
+    def cycle(self, l, r):
+        if l == self.L - 1:
+            return self._coarse(r)
+        act, D, w = self.act[l], self.D[l], self.omega
+        z = act * w * D * r
+        for _ in range(self.pre - 1):
+            z = act * (z + w * D * (r - self.A(l, z)))
+        t = act * (r - self.A(l, z))
+        zc = self.cycle(l + 1, restrict(t, self.masks[l + 1].shape, 2))
+        z = z + act * prolong(zc, self.masks[l], 2)
+        for _ in range(self.post):
+            z = act * (z + w * D * (r - self.A(l, z)))
+        return z
+
+    def apply(self, r_compressed):
+        r = to_dense(r_compressed, self.masks[0])
+        return to_compressed(self.cycle(0, r), self.masks[0])

@@ -151,6 +151,19 @@ def test_armadillo_parity(armadillo):
     assert f @ u == pytest.approx(f @ x_o, rel=1e-6)
 
 
+def test_multiplicative_vcycle_matches_numpy():
+    """VFEM_MG_VCYCLE (no reference counterpart) against its numpy restatement
+    (tests/structured_ref.MultiplicativeMG) on a lognormal-modulus voids domain."""
+    from tests import structured_ref as sr
+    d = domains.spheres(24, 2, 2, 4, seed=1, levels=3, lognormal_sigma=0.5)
+    ke = domains.hex8_stiffness()
+    A = api.assembleSystemMatrix(d.voxels, ke, d.fixed, 3, E=d.E)
+    M = sr.MultiplicativeMG(d.voxels, ke, d.fixed, 3, E=d.E)
+    r = np.random.default_rng(4).standard_normal(A.rows())
+    z_gpu = api.MultigridPreconditioner(A, "vcycle").solve(r)
+    assert rel(z_gpu, M.apply(r)) < 1e-10
+
+
 def test_per_voxel_modulus():
     """Extension with no reference counterpart: Ke_e = E_e Ke.  Uniform E = c scales
     the solution by 1/c; a random field keeps the operator symmetric and matches a

@@ -75,6 +75,7 @@ struct vfem_problem {
     // level-0 solver vectors (dense storage)
     double *f64 = nullptr, *x64 = nullptr, *p64 = nullptr, *Ap64 = nullptr;
     float *p32 = nullptr, *Ap32 = nullptr;
+    float* x32 = nullptr;  // mixed precision: FP32 solution correction since the last FP64 flush
     // coarsest dense inverse
     int64_t nc = 0;
     int32_t* freeDof = nullptr;
@@ -139,6 +140,7 @@ void freeProblem(vfem_problem* p) {
         cudaFree(l.r64); cudaFree(l.z64); cudaFree(l.t64); cudaFree(l.r32); cudaFree(l.z32); cudaFree(l.t32);
     }
     cudaFree(p->f64); cudaFree(p->x64); cudaFree(p->p64); cudaFree(p->Ap64); cudaFree(p->p32); cudaFree(p->Ap32);
+    cudaFree(p->x32);
     cudaFree(p->freeDof); cudaFree(p->Kinv64); cudaFree(p->Kinv32); cudaFree(p->cb64); cudaFree(p->cb32);
     cudaFree(p->S); cudaFree(p->rb.partials); cudaFree(p->rb.ticket); cudaFree(p->dComp);
     if (p->hS) cudaFreeHost(p->hS);
@@ -302,7 +304,7 @@ vfem_status createImpl(const uint8_t* vox, int nx, int ny, int nz, const double*
     }
     int64_t nv0 = p->L[0].nvec();
     CKP(dalloc(&p->f64, nv0)); CKP(dalloc(&p->x64, nv0)); CKP(dalloc(&p->p64, nv0)); CKP(dalloc(&p->Ap64, nv0));
-    CKP(dalloc(&p->p32, nv0)); CKP(dalloc(&p->Ap32, nv0));
+    CKP(dalloc(&p->p32, nv0)); CKP(dalloc(&p->Ap32, nv0)); CKP(dalloc(&p->x32, nv0));
     CKP(dalloc(&p->S, 1));
     CKP(dalloc(&p->rb.partials, 2 * (int64_t)kMaxRedBlocks));
     CKP(dalloc(&p->rb.ticket, 1));
@@ -491,7 +493,8 @@ int iteration(vfem_problem* p, const vfem_options& o, double** zOut64, float** z
         a.dot0 = DOT_X_OUT;
         a.epi = EPI_ALPHA;
         k += matvec<float>(p, a);
-        k += launchUpdateXR<double, float>(c, n, p->x64, l0.r32, p->p32, p->Ap32);
+        k += launchUpdateXR<float, float>(c, n, p->x32, l0.r32, p->p32, p->Ap32);
+        k += launchFlushX(c, n, p->x64, p->x32, 1);
         MatvecArgs<double> t = mvArgs<double>(p, 0, p->x64, l0.r64, MV_RESID);
         t.f = p->f64;
         t.y32 = l0.r32;
@@ -548,6 +551,7 @@ vfem_status solveImpl(vfem_problem* p, const vfem_options* optIn, bool haveX0, v
         launches += launchConvert<double, double>(p->stream, n, p->f64, l0.r64);
         if (mixed) launches += launchConvert<double, float>(p->stream, n, p->f64, l0.r32);
     }
+    if (mixed) launches += launchFill<float>(p->stream, n, p->x32, 0.f);
     launches += launchDots<double>(c, n, p->f64, p->f64, l0.r64, l0.r64, EPI_INIT, 0);
     if (mixed) {
         launches += precondition<float>(p, o, l0.r32, l0.z32, &z32, nullptr, EPI_RHO0);
@@ -586,6 +590,7 @@ vfem_status solveImpl(vfem_problem* p, const vfem_options* optIn, bool haveX0, v
         launches += cg.kernels;
         ++chunks;
     }
+    if (mixed) launches += launchFlushX(c, n, p->x64, p->x32, 0);  // fold any remaining FP32 correction
     CK(cudaEventRecord(e1, p->stream));
     CK(cudaEventSynchronize(e1));
     float ms = 0;
@@ -900,7 +905,7 @@ vfem_status vfem_profile_kernels(vfem_problem* p, int32_t reps, double* ms) {
                 case VFEM_K_UPDATE_XR_FP64:
                     return launchUpdateXR<double, double>(c, n, p->x64, l0.r64, p->p64, p->Ap64);
                 case VFEM_K_UPDATE_XR_MIXED:
-                    return launchUpdateXR<double, float>(c, n, p->x64, l0.r32, p->p32, p->Ap32);
+                    return launchUpdateXR<float, float>(c, n, p->x32, l0.r32, p->p32, p->Ap32);
                 case VFEM_K_UPDATE_P_FP64:
                     return launchUpdateP<double>(c, n, p->p64, l0.z64, 0);
                 case VFEM_K_UPDATE_P_FP32:

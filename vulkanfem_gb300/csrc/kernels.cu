@@ -149,6 +149,31 @@ __device__ __forceinline__ bool trueResidualDue(const Scalars* S) {
            (S->delta2 > 0.0 && S->rr < S->delta2 * S->rrLast);
 }
 
+// Per-thread dot-product accumulator.  FP64 vectors accumulate in FP64.  FP32
+// vectors accumulate in FP32 with Kahan compensation and are converted to FP64
+// once per thread, before the FP64 block and grid reduction: on GB300 the FP64
+// pipe is ~1/64 of FP32, so per-element FP64 conversions and FMAs would bound
+// the FP32 kernels.
+template <typename T>
+struct DotAcc;
+template <>
+struct DotAcc<double> {
+    double s = 0.0;
+    __device__ __forceinline__ void add(double v) { s += v; }
+    __device__ __forceinline__ double get() const { return s; }
+};
+template <>
+struct DotAcc<float> {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float v) {
+        const float y = v - c;
+        const float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ double get() const { return (double)s - (double)c; }
+};
+
 template <typename T>
 struct Ks {
     T v[45];
@@ -225,8 +250,38 @@ struct KP<T, false> {
     typedef Kd<T> type;
 };
 
-constexpr int kSuElems = 2 * (MV_TY + 1) * (MV_TX + 1) * 3;
-constexpr int kSyElems = MV_TY * MV_TX * 18;
+// Shared-memory node slots are padded to 4 values (x, y, z, unused) so that a
+// node moves with one 16-byte (float) or two 16-byte (double) accesses.
+constexpr int kSuElems = 2 * (MV_TY + 1) * (MV_TX + 1) * 4;
+constexpr int kSyElems = MV_TY * MV_TX * 6 * 4;
+
+template <typename T>
+__device__ __forceinline__ void stSlot(T* p, T a, T b, T c);
+template <>
+__device__ __forceinline__ void stSlot<float>(float* p, float a, float b, float c) {
+    *reinterpret_cast<float4*>(p) = make_float4(a, b, c, 0.f);
+}
+template <>
+__device__ __forceinline__ void stSlot<double>(double* p, double a, double b, double c) {
+    reinterpret_cast<double2*>(p)[0] = make_double2(a, b);
+    reinterpret_cast<double2*>(p)[1] = make_double2(c, 0.0);
+}
+template <typename T>
+__device__ __forceinline__ void ldSlot(const T* p, T& a, T& b, T& c);
+template <>
+__device__ __forceinline__ void ldSlot<float>(const float* p, float& a, float& b, float& c) {
+    const float4 v = *reinterpret_cast<const float4*>(p);
+    a = v.x;
+    b = v.y;
+    c = v.z;
+}
+template <>
+__device__ __forceinline__ void ldSlot<double>(const double* p, double& a, double& b, double& c) {
+    const double2 v0 = reinterpret_cast<const double2*>(p)[0], v1 = reinterpret_cast<const double2*>(p)[1];
+    a = v0.x;
+    b = v0.y;
+    c = v1.x;
+}
 
 // Element-by-element product on a 2.5-D tile.  A block of 32 x 8 threads marches
 // up a z-range; at each element layer thread (tx,ty) computes the element whose
@@ -235,8 +290,13 @@ constexpr int kSyElems = MV_TY * MV_TX * 18;
 // threads' elements.  Element outputs pass through shared memory once; each
 // owned node sums its four in-layer contributions for the bottom face (node
 // layer k) and the top face (node layer k+1), so no atomics are needed.
+// The march is software-pipelined: while layer k is computed, the node values
+// of layer k+2, the modulus of element layer k+1 and the owned node's flags
+// are already in flight to registers.  The 33 x 9 node tile of a layer is
+// loaded without integer division: every thread loads its own slot, row 8
+// comes from the ty == 0 threads and column 32 from nine threads of row 1.
 template <typename T, bool STRUCT>
-__global__ void __launch_bounds__(MV_TX* MV_TY)
+__global__ void __launch_bounds__(MV_TX* MV_TY, STRUCT ? (sizeof(T) == 4 ? 4 : 2) : 1)
     kMatvec(MatvecArgs<T> a, const typename KP<T, STRUCT>::type kp, Scalars* S, RedBuf rb) {
     if (a.checkDone && S->done) return;
     if (a.condTrue && !trueResidualDue(S)) return;
@@ -244,55 +304,83 @@ __global__ void __launch_bounds__(MV_TX* MV_TY)
     T* su = reinterpret_cast<T*>(smemRaw);
     T* sy = su + kSuElems;
     const Grid g = a.g;
-    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * MV_TX + tx;
+    const int tx = threadIdx.x, ty = threadIdx.y;
     const int x0 = blockIdx.x * (MV_TX - 1), y0 = blockIdx.y * (MV_TY - 1), z0 = blockIdx.z * MV_ZC;
     const int zend = min(z0 + MV_ZC, g.nz);
+    const int64_t plane = (int64_t)g.nx * g.ny;
     const int ecx = x0 + tx - 1, ecy = y0 + ty - 1;
     const int onx = x0 + tx, ony = y0 + ty;
     const bool owner = (tx < MV_TX - 1) && (ty < MV_TY - 1) && onx < g.nx && ony < g.ny;
     const bool ecxy = ecx >= 0 && ecx < g.ex && ecy >= 0 && ecy < g.ey;
+    const int eCol = ecy * g.nx + ecx;   // in-plane offsets fit in 32 bits for every accepted grid
+    const int oCol = ony * g.nx + onx;
     const T sc = (T)a.scale;
-#define SU(b, iy, ix, c) su[((((b) * (MV_TY + 1)) + (iy)) * (MV_TX + 1) + (ix)) * 3 + (c)]
-#define SY(iy, ix, k) sy[((iy) * MV_TX + (ix)) * 18 + (k)]
-    auto load = [&](int zl) {
-        const int b = zl & 1;
-        for (int i = tid; i < (MV_TX + 1) * (MV_TY + 1); i += MV_TX * MV_TY) {
-            const int ix = i % (MV_TX + 1), iy = i / (MV_TX + 1);
-            const int gx = x0 - 1 + ix, gy = y0 - 1 + iy;
-            T v0 = T(0), v1 = T(0), v2 = T(0);
-            if (gx >= 0 && gx < g.nx && gy >= 0 && gy < g.ny && zl >= 0 && zl < g.nz) {
-                const T* p = a.x + 3 * g.store(gx, gy, zl);
-                v0 = p[0];
-                v1 = p[1];
-                v2 = p[2];
-            }
-            SU(b, iy, ix, 0) = v0;
-            SU(b, iy, ix, 1) = v1;
-            SU(b, iy, ix, 2) = v2;
+    // Extra tile slots: row MV_TY (ty == 0 threads), column MV_TX (row-1 threads tx <= MV_TY).
+    const bool hasR = ty == 0, hasC = (ty == 1) && (tx <= MV_TY);
+    const int rX = x0 - 1 + tx, rY = y0 - 1 + MV_TY;
+    const int cX = x0 - 1 + MV_TX, cY = y0 - 1 + tx;
+    const bool ok0 = ecx >= 0 && ecx < g.nx && ecy >= 0 && ecy < g.ny;
+    const bool okR = hasR && rX >= 0 && rX < g.nx && rY >= 0 && rY < g.ny;
+    const bool okC = hasC && cX >= 0 && cX < g.nx && cY >= 0 && cY < g.ny;
+#define SU(b, iy, ix) (su + (((((b) * (MV_TY + 1)) + (iy)) * (MV_TX + 1) + (ix)) << 2))
+#define SY(k, iy, ix) (sy + (((((k) * MV_TY) + (iy)) * MV_TX + (ix)) << 2))
+    T pf[9];
+    auto gload = [&](int zl) {
+        const bool zok = zl >= 0 && zl < g.nz;
+        const int64_t zoff = (int64_t)zl * plane;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) pf[i] = T(0);
+        if (ok0 && zok) {
+            const T* p = a.x + 3 * ((int64_t)eCol + zoff);
+            pf[0] = p[0]; pf[1] = p[1]; pf[2] = p[2];
+        }
+        if (okR && zok) {
+            const T* p = a.x + 3 * ((int64_t)(rY * g.nx + rX) + zoff);
+            pf[3] = p[0]; pf[4] = p[1]; pf[5] = p[2];
+        }
+        if (okC && zok) {
+            const T* p = a.x + 3 * ((int64_t)(cY * g.nx + cX) + zoff);
+            pf[6] = p[0]; pf[7] = p[1]; pf[8] = p[2];
         }
     };
+    auto sstore = [&](int zl) {
+        const int b = zl & 1;
+        stSlot<T>(SU(b, ty, tx), pf[0], pf[1], pf[2]);
+        if (hasR) stSlot<T>(SU(b, MV_TY, tx), pf[3], pf[4], pf[5]);
+        if (hasC) stSlot<T>(SU(b, tx, MV_TX), pf[6], pf[7], pf[8]);
+    };
+    auto eload = [&](int k) -> float {
+        return (ecxy && k >= 0 && k < g.ez) ? a.E[(int64_t)eCol + (int64_t)k * plane] : 0.f;
+    };
+    auto fload = [&](int k) -> uint8_t {
+        return (owner && k >= z0 && k < zend) ? a.flags[(int64_t)oCol + (int64_t)k * plane] : (uint8_t)0;
+    };
     T acc[3] = {T(0), T(0), T(0)};
-    double d0 = 0.0, d1 = 0.0;
-    load(z0 - 1);
+    DotAcc<T> d0, d1;
+    gload(z0 - 1);
+    sstore(z0 - 1);
+    gload(z0);
+    float Enext = eload(z0 - 1);
+    uint8_t flNext = fload(z0 - 1);
     for (int k = z0 - 1; k < zend; ++k) {
-        load(k + 1);
+        sstore(k + 1);
+        const float Ee = Enext;
+        const uint8_t fl = flNext;
         __syncthreads();
-        // x at the owned node of layer k, read now: the next iteration's load
+        gload(k + 2);           // consumed by the next iteration
+        Enext = eload(k + 1);
+        flNext = fload(k + 1);
+        // x at the owned node of layer k, read now: the next iteration's store
         // overwrites this layer's buffer without waiting for the output phase.
         T xo[3];
-#pragma unroll
-        for (int c = 0; c < 3; ++c) xo[c] = SU(k & 1, ty + 1, tx + 1, c);
+        ldSlot<T>(SU(k & 1, ty + 1, tx + 1), xo[0], xo[1], xo[2]);
         T ye[24];
-        float Ee = 0.f;
-        if (ecxy && k >= 0 && k < g.ez) Ee = a.E[g.store(ecx, ecy, k)];
         if (Ee != 0.f) {
             T u[24];
 #pragma unroll
             for (int n = 0; n < 8; ++n) {
                 const int dx = n & 1, dy = (n >> 1) & 1, dz = n >> 2;
-                const int b = (k + dz) & 1;
-#pragma unroll
-                for (int c = 0; c < 3; ++c) u[3 * n + c] = SU(b, ty + dy, tx + dx, c);
+                ldSlot<T>(SU((k + dz) & 1, ty + dy, tx + dx), u[3 * n], u[3 * n + 1], u[3 * n + 2]);
             }
             if constexpr (STRUCT) elemStruct<T>(u, ye, kp, sc * (T)Ee);
             else elemDense<T>(u, ye, kp, sc * (T)Ee);
@@ -300,26 +388,40 @@ __global__ void __launch_bounds__(MV_TX* MV_TY)
 #pragma unroll
             for (int i = 0; i < 24; ++i) ye[i] = T(0);
         }
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            SY(ty, tx, 0 + c) = ye[0 + c];    // a = 0
-            SY(ty, tx, 3 + c) = ye[3 + c];    // a = 1
-            SY(ty, tx, 6 + c) = ye[6 + c];    // a = 2
-            SY(ty, tx, 9 + c) = ye[12 + c];   // a = 4
-            SY(ty, tx, 12 + c) = ye[15 + c];  // a = 5
-            SY(ty, tx, 15 + c) = ye[18 + c];  // a = 6
-        }
+        stSlot<T>(SY(0, ty, tx), ye[0], ye[1], ye[2]);     // a = 0
+        stSlot<T>(SY(1, ty, tx), ye[3], ye[4], ye[5]);     // a = 1
+        stSlot<T>(SY(2, ty, tx), ye[6], ye[7], ye[8]);     // a = 2
+        stSlot<T>(SY(3, ty, tx), ye[12], ye[13], ye[14]);  // a = 4
+        stSlot<T>(SY(4, ty, tx), ye[15], ye[16], ye[17]);  // a = 5
+        stSlot<T>(SY(5, ty, tx), ye[18], ye[19], ye[20]);  // a = 6
         __syncthreads();
         if (owner) {
-            T lo[3], hi[3];
+            T lo[3], hi[3], q[3];
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-                lo[c] = ye[9 + c] + SY(ty, tx + 1, 6 + c) + SY(ty + 1, tx, 3 + c) + SY(ty + 1, tx + 1, 0 + c);
-                hi[c] = ye[21 + c] + SY(ty, tx + 1, 15 + c) + SY(ty + 1, tx, 12 + c) + SY(ty + 1, tx + 1, 9 + c);
+                lo[c] = ye[9 + c];
+                hi[c] = ye[21 + c];
             }
+            ldSlot<T>(SY(2, ty, tx + 1), q[0], q[1], q[2]);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) lo[c] += q[c];
+            ldSlot<T>(SY(1, ty + 1, tx), q[0], q[1], q[2]);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) lo[c] += q[c];
+            ldSlot<T>(SY(0, ty + 1, tx + 1), q[0], q[1], q[2]);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) lo[c] += q[c];
+            ldSlot<T>(SY(5, ty, tx + 1), q[0], q[1], q[2]);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) hi[c] += q[c];
+            ldSlot<T>(SY(4, ty + 1, tx), q[0], q[1], q[2]);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) hi[c] += q[c];
+            ldSlot<T>(SY(3, ty + 1, tx + 1), q[0], q[1], q[2]);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) hi[c] += q[c];
             if (k >= z0) {
-                const int64_t s = g.store(onx, ony, k);
-                const uint8_t fl = a.flags[s];
+                const int64_t s = (int64_t)oCol + (int64_t)k * plane;
                 const bool fixed = (fl & FLAG_FIXED) != 0;
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
@@ -336,10 +438,10 @@ __global__ void __launch_bounds__(MV_TX* MV_TY)
                     }
                     a.y[3 * s + c] = out;
                     if (a.y32) a.y32[3 * s + c] = (float)out;
-                    if (a.dot0 == DOT_X_OUT) d0 += (double)xv * (double)out;
-                    else if (a.dot0 == DOT_OUT_OUT) d0 += (double)out * (double)out;
-                    else if (a.dot0 == DOT_F_OUT) d0 += (double)fv * (double)out;
-                    if (a.dot1) d1 += (double)out * (double)a.aux[3 * s + c];
+                    if (a.dot0 == DOT_X_OUT) d0.add(xv * out);
+                    else if (a.dot0 == DOT_OUT_OUT) d0.add(out * out);
+                    else if (a.dot0 == DOT_F_OUT) d0.add(fv * out);
+                    if (a.dot1) d1.add(out * a.aux[3 * s + c]);
                 }
             }
 #pragma unroll
@@ -349,7 +451,7 @@ __global__ void __launch_bounds__(MV_TX* MV_TY)
 #undef SU
 #undef SY
     if (a.epi != EPI_NONE) {
-        double v[2] = {d0, d1}, t[2];
+        double v[2] = {d0.get(), d1.get()}, t[2];
         if (gridReduce<MV_TX * MV_TY, 2>(v, rb, t)) applyEpi(a.epi, S, t[0], t[1]);
     }
 }
@@ -440,7 +542,7 @@ __global__ void __launch_bounds__(256)
     if (checkDone && S->done) return;
     const int fx = blockIdx.x * 32 + threadIdx.x, fy = blockIdx.y * 8 + threadIdx.y;
     const bool valid = fx < gf.nx && fy < gf.ny;
-    double d0 = 0.0, d1 = 0.0;
+    DotAcc<T> d0, d1;
     if (valid) {
         for (int fz = blockIdx.z * PZ; fz < min(gf.nz, (int)(blockIdx.z + 1) * PZ); ++fz) {
             const int64_t s = gf.store(fx, fy, fz);
@@ -462,14 +564,14 @@ __global__ void __launch_bounds__(256)
             if (epi != EPI_NONE) {
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
-                    d0 += (double)r[c] * (double)out[c];
-                    if (aux) d1 += (double)out[c] * (double)aux[3 * s + c];
+                    d0.add(r[c] * out[c]);
+                    if (aux) d1.add(out[c] * aux[3 * s + c]);
                 }
             }
         }
     }
     if (epi != EPI_NONE) {
-        double v[2] = {d0, d1}, t[2];
+        double v[2] = {d0.get(), d1.get()}, t[2];
         if (gridReduce<256, 2>(v, rb, t)) applyEpi(epi, S, t[0], t[1]);
     }
 }
@@ -530,31 +632,78 @@ __global__ void __launch_bounds__(256) kGemv(const T* __restrict__ K, int64_t n,
     if (lane == 0) zc[freeDof[row]] = acc;
 }
 
+// 4-wide vector loads/stores of the flat vector kernels (float4; two double2).
+template <typename T>
+struct V4;
+template <>
+struct V4<float> {
+    static __device__ __forceinline__ void ld(const float* p, float (&v)[4]) {
+        const float4 t = *reinterpret_cast<const float4*>(p);
+        v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+    }
+    static __device__ __forceinline__ void st(float* p, const float (&v)[4]) {
+        *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+    }
+};
+template <>
+struct V4<double> {
+    static __device__ __forceinline__ void ld(const double* p, double (&v)[4]) {
+        const double2 a = reinterpret_cast<const double2*>(p)[0], b = reinterpret_cast<const double2*>(p)[1];
+        v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+    }
+    static __device__ __forceinline__ void st(double* p, const double (&v)[4]) {
+        reinterpret_cast<double2*>(p)[0] = make_double2(v[0], v[1]);
+        reinterpret_cast<double2*>(p)[1] = make_double2(v[2], v[3]);
+    }
+};
+
+// x += alpha p; r -= alpha Ap; r.r.  TX = double is the FP64 solution; TX = float
+// is the mixed-precision correction accumulated since the last flush.
 template <typename TX, typename TV>
 __global__ void __launch_bounds__(256) kUpdateXR(int64_t n, TX* __restrict__ x, TV* __restrict__ r,
                                                  const TV* __restrict__ p, const TV* __restrict__ Ap, Scalars* S,
                                                  RedBuf rb) {
     if (S->done) return;
-    const double alpha = S->alpha;
-    const TV av = (TV)alpha;
-    double acc = 0.0;
-    TV part = TV(0);
-    int cnt = 0;
-    for (int64_t i = blockIdx.x * (int64_t)NT + threadIdx.x; i < n; i += (int64_t)gridDim.x * NT) {
-        const TV pi = p[i], api = Ap[i];
-        x[i] = (TX)((TX)x[i] + (TX)alpha * (TX)pi);
-        const TV ri = r[i] - av * api;
-        r[i] = ri;
-        part = fma(ri, ri, part);
-        if (++cnt == 8) {  // short partial sums in the vector type, accumulated in FP64
-            acc += (double)part;
-            part = TV(0);
-            cnt = 0;
+    const TX ax = (TX)S->alpha;
+    const TV av = (TV)S->alpha;
+    DotAcc<TV> acc;
+    const int64_t tid = blockIdx.x * (int64_t)NT + threadIdx.x, stride = (int64_t)gridDim.x * NT;
+    const int64_t n4 = n / 4;
+    for (int64_t q = tid; q < n4; q += stride) {
+        TX xv[4];
+        TV rv[4], pv[4], av4[4];
+        V4<TX>::ld(x + 4 * q, xv);
+        V4<TV>::ld(r + 4 * q, rv);
+        V4<TV>::ld(p + 4 * q, pv);
+        V4<TV>::ld(Ap + 4 * q, av4);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            xv[k] = fma(ax, (TX)pv[k], xv[k]);
+            rv[k] = fma(-av, av4[k], rv[k]);
+            acc.add(rv[k] * rv[k]);
         }
+        V4<TX>::st(x + 4 * q, xv);
+        V4<TV>::st(r + 4 * q, rv);
     }
-    acc += (double)part;
-    double v[1] = {acc}, t[1];
+    for (int64_t i = 4 * n4 + tid; i < n; i += stride) {
+        x[i] = fma(ax, (TX)p[i], x[i]);
+        const TV ri = fma(-av, Ap[i], r[i]);
+        r[i] = ri;
+        acc.add(ri * ri);
+    }
+    double v[1] = {acc.get()}, t[1];
     if (gridReduce<NT, 1>(v, rb, t)) applyEpi(EPI_CONV, S, t[0], 0.0);
+}
+
+// Mixed precision: fold the FP32 solution correction into the FP64 solution.
+// conditional = 1: only when an FP64 true-residual pass follows in this iteration.
+__global__ void __launch_bounds__(256) kFlushX(int64_t n, double* __restrict__ x64, float* __restrict__ x32,
+                                               const Scalars* S, int conditional) {
+    if (conditional && (S->done || !trueResidualDue(S))) return;
+    for (int64_t i = blockIdx.x * (int64_t)NT + threadIdx.x; i < n; i += (int64_t)gridDim.x * NT) {
+        x64[i] += (double)x32[i];
+        x32[i] = 0.f;
+    }
 }
 
 template <typename T>
@@ -562,8 +711,17 @@ __global__ void __launch_bounds__(256) kUpdateP(int64_t n, T* __restrict__ p, co
                                                 const Scalars* S, int first) {
     if (S->done) return;
     const T beta = first ? T(0) : (T)S->beta;
-    for (int64_t i = blockIdx.x * (int64_t)NT + threadIdx.x; i < n; i += (int64_t)gridDim.x * NT)
-        p[i] = first ? z[i] : fma(beta, p[i], z[i]);
+    const int64_t tid = blockIdx.x * (int64_t)NT + threadIdx.x, stride = (int64_t)gridDim.x * NT;
+    const int64_t n4 = n / 4;
+    for (int64_t q = tid; q < n4; q += stride) {
+        T pv[4], zv[4];
+        V4<T>::ld(p + 4 * q, pv);
+        V4<T>::ld(z + 4 * q, zv);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) pv[k] = fma(beta, pv[k], zv[k]);
+        V4<T>::st(p + 4 * q, pv);
+    }
+    for (int64_t i = 4 * n4 + tid; i < n; i += stride) p[i] = fma(beta, p[i], z[i]);
 }
 
 template <typename T>
@@ -571,12 +729,12 @@ __global__ void __launch_bounds__(256) kDots(int64_t n, const T* __restrict__ a,
                                              const T* __restrict__ c, const T* __restrict__ d, int epi, Scalars* S,
                                              RedBuf rb, int checkDone) {
     if (checkDone && S->done) return;
-    double s0 = 0.0, s1 = 0.0;
+    DotAcc<T> s0, s1;
     for (int64_t i = blockIdx.x * (int64_t)NT + threadIdx.x; i < n; i += (int64_t)gridDim.x * NT) {
-        if (a) s0 += (double)a[i] * (double)b[i];
-        if (c) s1 += (double)c[i] * (double)d[i];
+        if (a) s0.add(a[i] * b[i]);
+        if (c) s1.add(c[i] * d[i]);
     }
-    double v[2] = {s0, s1}, t[2];
+    double v[2] = {s0.get(), s1.get()}, t[2];
     if (gridReduce<NT, 2>(v, rb, t)) applyEpi(epi, S, t[0], t[1]);
 }
 
@@ -744,6 +902,11 @@ int launchUpdateXR(const LaunchCtx& c, int64_t n, TX* x, TV* r, const TV* p, con
     return 1;
 }
 
+int launchFlushX(const LaunchCtx& c, int64_t n, double* x64, float* x32, int conditional) {
+    kFlushX<<<flatBlocks(n), NT, 0, c.stream>>>(n, x64, x32, c.S, conditional);
+    return 1;
+}
+
 template <typename T>
 int launchUpdateP(const LaunchCtx& c, int64_t n, T* p, const T* z, int first) {
     kUpdateP<T><<<flatBlocks(n), NT, 0, c.stream>>>(n, p, z, c.S, first);
@@ -896,6 +1059,7 @@ INST_T(double)
 INST_T(float)
 template int launchUpdateXR<double, double>(const LaunchCtx&, int64_t, double*, double*, const double*, const double*);
 template int launchUpdateXR<double, float>(const LaunchCtx&, int64_t, double*, float*, const float*, const float*);
+template int launchUpdateXR<float, float>(const LaunchCtx&, int64_t, float*, float*, const float*, const float*);
 template int launchConvert<double, float>(cudaStream_t, int64_t, const double*, float*);
 template int launchConvert<float, double>(cudaStream_t, int64_t, const float*, double*);
 template int launchConvert<double, double>(cudaStream_t, int64_t, const double*, double*);

@@ -122,6 +122,9 @@ int launchCoarseSolve(const LaunchCtx& c, const T* Kinv, int64_t n, const int32_
 // x += alpha p ; r -= alpha Ap ; rr -> EPI_CONV
 template <typename TX, typename TV>
 int launchUpdateXR(const LaunchCtx& c, int64_t n, TX* x, TV* r, const TV* p, const TV* Ap);
+// x64 += x32; x32 = 0 (mixed precision).  conditional: only in iterations that
+// recompute the FP64 true residual.
+int launchFlushX(const LaunchCtx& c, int64_t n, double* x64, float* x32, int conditional);
 // p = z + beta p
 template <typename T>
 int launchUpdateP(const LaunchCtx& c, int64_t n, T* p, const T* z, int first);
