@@ -115,7 +115,8 @@ def fixed_dilate(fine_fixed, coarse_shape, div=2):
 class MultiplicativeMG:
     """numpy restatement of the library's multiplicative V-cycle
     (VFEM_MG_VCYCLE): rediscretised level operators 2^l sum_e E_e Ke (coarse
-    elements carry the mean modulus of their used children), damped Jacobi on
+    elements carry the volume average of their children's modulus, empty
+    children counting as 0), damped Jacobi on
     their diagonals, full weighting / trilinear prolongation, fixed DOFs masked
     on every level (fixed sets dilated from the finest), dense coarsest solve."""
 
@@ -135,7 +136,7 @@ class MultiplicativeMG:
             blk = pad.reshape(cz, 2, cy, 2, cx, 2)
             cnt = (blk > 0).sum(axis=(1, 3, 5))
             sm = blk.sum(axis=(1, 3, 5))
-            Ec = np.where(cnt > 0, (sm / np.maximum(cnt, 1)).astype(np.float32).astype(float), 0.0)
+            Ec = np.where(cnt > 0, (sm / 8.0).astype(np.float32).astype(float), 0.0)
             self.Es.append(Ec)
             self.masks.append(used_mask(Ec > 0))
             self.fixeds.append(fixed_dilate(self.fixeds[-1], self.masks[-1].shape, 2))

@@ -1,0 +1,90 @@
+"""GPU tests of the learned part (BF16 U-Net kernels in csrc/unet.cu).
+
+Forward outputs and parameter gradients of the CUDA kernels are checked against
+the numpy restatement (tests/unet_ref.py, same BF16 rounding points, float64
+sums): relative L2 error <= 2e-2 for the output and for every layer's weight
+and bias gradient (BF16 storage, FP32 tensor-core accumulation).
+"""
+import numpy as np
+import pytest
+
+from tests import unet_ref as U
+from vulkanfem_gb300 import domains, learned
+
+pytestmark = pytest.mark.gpu
+
+TOL = 2e-2
+
+
+def _rel(a, b):
+    nb = np.linalg.norm(b)
+    return float(np.linalg.norm(a - b) / nb) if nb > 0 else float(np.linalg.norm(a))
+
+
+def _problem(n, seed):
+    rng = np.random.default_rng(seed)
+    x = np.zeros((n, n, n, 16), np.float32)
+    x[..., :6] = rng.standard_normal((n, n, n, 6)) * 0.5
+    t = (rng.standard_normal((n, n, n, 3)) * 0.1).astype(np.float32)
+    m = (rng.random((n, n, n)) < 0.8).astype(np.float32)
+    return x, t, m
+
+
+def test_unet_forward_and_gradients_match_numpy():
+    U.ROUND = True
+    n = 16
+    p = U.init_params(3)
+    net = learned.UNet(n, p)
+    x, t, m = _problem(n, 0)
+    y_gpu = net.forward(x)
+    loss_ref, g_ref, y_ref = U.loss_and_grads(p.astype(np.float64), x.astype(np.float64), t.astype(np.float64),
+                                              m.astype(np.float64))
+    assert _rel(y_gpu, y_ref[..., :3]) < TOL
+    loss, g = net.train_batch(x[None], t[None], m[None], 0.0, want_grads=True)
+    assert loss == pytest.approx(loss_ref, rel=TOL)
+    lay, _ = U.param_layout()
+    for l, ((w0, w1), (b0, b1)) in enumerate(lay):
+        assert _rel(g[w0:w1], g_ref[w0:w1]) < TOL, ("weights", l, _rel(g[w0:w1], g_ref[w0:w1]))
+        assert _rel(g[b0:b1], g_ref[b0:b1]) < TOL, ("bias", l, _rel(g[b0:b1], g_ref[b0:b1]))
+    # batch of two identical samples: same mean gradient
+    _, g2 = net.train_batch(np.stack([x, x]), np.stack([t, t]), np.stack([m, m]), 0.0, want_grads=True)
+    assert _rel(g2, g) < 1e-5
+
+
+@pytest.fixture(scope="module")
+def trained():
+    """A net trained with the library's own kernels on 12 solver outputs (24^3)."""
+    X, T, M = learned.generate(12, n=24, seed0=100, levels=3)
+    net = learned.UNet(X.shape[1])
+    l0 = net.train_batch(X[:4], T[:4], M[:4], 0.0)[0]
+    hist = learned.train(net, X, T, M, epochs=10, batch=4, lr=1e-3)
+    l1 = net.train_batch(X[:4], T[:4], M[:4], 0.0)[0]
+    yield net, l0, l1, hist
+    net.close()
+
+
+def test_unet_training_reduces_loss(trained):
+    _, l0, l1, hist = trained
+    assert l1 < 0.8 * l0, (l0, l1, hist)
+
+
+def test_warm_start_reaches_the_same_answer(trained):
+    """A warm start only changes the starting point: the solve still stops on the
+    same FP64 relative residual and returns the cold solve's answer to the
+    tolerance.  (Measured on 64^3 fields the learned start saves no iterations;
+    the iteration count may move by a few either way.)"""
+    from vulkanfem_gb300 import api
+    net = trained[0]
+    ke = domains.hex8_stiffness()
+    for seed in (50001, 50002):
+        d = domains.training_field(24, seed=seed, levels=3)
+        A = api.assembleSystemMatrix(d.voxels, ke, d.fixed, 3)
+        f = d.load_vector()
+        u0 = learned.warm_start(net, d, A, f)
+        assert np.all(u0.reshape(-1, 3)[d.fixed] == 0)
+        uc, cold = A.solve(f, precision="mixed")
+        uw, warm = A.solve(f, u0=u0, precision="mixed")
+        A.close()
+        assert warm["rel_residual"] < 1e-6 and cold["rel_residual"] < 1e-6
+        assert _rel(uw, uc) < 1e-4
+        assert warm["iterations"] <= 1.2 * cold["iterations"] + 5, (cold["iterations"], warm["iterations"])

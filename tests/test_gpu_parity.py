@@ -151,6 +151,24 @@ def test_armadillo_parity(armadillo):
     assert f @ u == pytest.approx(f @ x_o, rel=1e-6)
 
 
+def test_per_voxel_modulus_parity_with_oracle():
+    """Reference-mode hierarchy, product, preconditioner and solve with a lognormal
+    per-voxel modulus, against the oracle's same extension."""
+    d = domains.spheres(24, 3, 2, 5, seed=3, levels=3, lognormal_sigma=0.5)
+    ke = domains.hex8_stiffness()
+    o = oracle.Oracle(d.voxels, ke, d.fixed, 3, E=d.E)
+    A = api.assembleSystemMatrix(d.voxels, ke, d.fixed, 3, E=d.E)
+    for lv in range(o.num_levels):
+        assert rel(A.inverse_diagonal(lv), o.inv_diag(lv)) < OP_TOL
+    x = np.random.default_rng(6).standard_normal(A.rows())
+    assert rel(A @ x, o.matvec(x)) < OP_TOL
+    assert rel(api.MultigridPreconditioner(A).solve(x), o.precond(x)) < 1e-10
+    f = d.load_vector()
+    u, st = A.solve(f)
+    xo, ito, _ = o.pcg(f)
+    assert abs(st["iterations"] - ito) <= 1 and rel(u, xo) < 1e-5
+
+
 def test_multiplicative_vcycle_matches_numpy():
     """VFEM_MG_VCYCLE (no reference counterpart) against its numpy restatement
     (tests/structured_ref.MultiplicativeMG) on a lognormal-modulus voids domain."""

@@ -3,7 +3,9 @@
 The solver itself is the C-ABI CUDA library ``libvfem.so`` (``csrc/``, declared
 in ``include/vfem.h``); this package builds it in-tree and mirrors the
 reference's solve-path interface on top of it (``api``), plus the seeded
-synthetic domains (``domains``) and the reference's ``.dat`` readers (``io``).
+synthetic domains (``domains``) and the reference's ``.dat`` readers and
+writers (``inout``; ``python -m vulkanfem_gb300 <model>.dat`` is the reference's
+command-line driver).
 """
 from .api import (  # noqa: F401
     MatrixFreeSparse, MultigridPreconditioner, VfemError, applyBoundaryConditions, assembleSystemMatrix,

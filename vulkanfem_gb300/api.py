@@ -43,6 +43,9 @@ EXPORTED = (
     "vfem_restrict", "vfem_interpolate", "vfem_inverse_diagonal", "vfem_fixed_nodes",
     "vfem_kernel_launch_count", "vfem_last_error_message", "vfem_profile_kernels",
     "vfem_apply_operator_device_noalloc",
+    # learned warm start (include/vfem_net.h)
+    "vfem_net_create", "vfem_net_destroy", "vfem_net_num_params", "vfem_net_set_params", "vfem_net_get_params",
+    "vfem_net_forward", "vfem_net_train_batch", "vfem_net_last_error_message",
 )
 
 KERNEL_CLASSES = ("matvec_fp64", "matvec_fp32", "restrict_fp64", "restrict_fp32", "prolong_fp64", "prolong_fp32",

@@ -39,6 +39,7 @@ struct DevLevel {
     double scale = 1.0;
     int64_t nused = 0, nelem = 0;
     float* E = nullptr;
+    float* Ev = nullptr;  // multiplicative-cycle modulus (volume average; aliases E on the finest level)
     uint8_t* flags = nullptr;
     int32_t* nodeStore = nullptr;
     double* dinv64 = nullptr;
@@ -81,6 +82,8 @@ struct vfem_problem {
     int32_t* freeDof = nullptr;
     double* Kinv64 = nullptr;
     float* Kinv32 = nullptr;
+    double* KinvV64 = nullptr;  // multiplicative cycle's coarsest inverse (volume-averaged modulus)
+    float* KinvV32 = nullptr;
     double* cb64 = nullptr;
     float* cb32 = nullptr;
     // reductions / scalars
@@ -135,6 +138,7 @@ void freeProblem(vfem_problem* p) {
     for (auto& kv : p->graphs)
         if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
     for (auto& l : p->L) {
+        if (l.Ev != l.E) cudaFree(l.Ev);
         cudaFree(l.E); cudaFree(l.flags); cudaFree(l.nodeStore);
         cudaFree(l.dinv64); cudaFree(l.dinv32); cudaFree(l.dinvR64); cudaFree(l.dinvR32);
         cudaFree(l.r64); cudaFree(l.z64); cudaFree(l.t64); cudaFree(l.r32); cudaFree(l.z32); cudaFree(l.t32);
@@ -142,6 +146,7 @@ void freeProblem(vfem_problem* p) {
     cudaFree(p->f64); cudaFree(p->x64); cudaFree(p->p64); cudaFree(p->Ap64); cudaFree(p->p32); cudaFree(p->Ap32);
     cudaFree(p->x32);
     cudaFree(p->freeDof); cudaFree(p->Kinv64); cudaFree(p->Kinv32); cudaFree(p->cb64); cudaFree(p->cb32);
+    cudaFree(p->KinvV64); cudaFree(p->KinvV32);
     cudaFree(p->S); cudaFree(p->rb.partials); cudaFree(p->rb.ticket); cudaFree(p->dComp);
     if (p->hS) cudaFreeHost(p->hS);
     if (p->hIn) cudaFreeHost(p->hIn);
@@ -151,6 +156,9 @@ void freeProblem(vfem_problem* p) {
 }
 
 LaunchCtx ctx(vfem_problem* p) { return LaunchCtx{p->stream, p->S, p->rb}; }
+
+vfem_status invertCoarse(vfem_problem* p, const int32_t* dFreeNode, const float* E, double scale, double* K64,
+                         float* K32);
 
 vfem_status buildCoarse(vfem_problem* p) {
     const HostLevel& hc = p->H.L.back();
@@ -167,25 +175,37 @@ vfem_status buildCoarse(vfem_problem* p) {
     CK(upload(&dFreeNode, p->H.coarseFreeNode));
     CK(dalloc(&p->Kinv64, n * n));
     CK(dalloc(&p->Kinv32, n * n));
+    CK(dalloc(&p->KinvV64, n * n));
+    CK(dalloc(&p->KinvV32, n * n));
     CK(dalloc(&p->cb64, n));
     CK(dalloc(&p->cb32, n));
-    // Kc = 2^(L-1+skip) sum_e E_e Ke on the free DOFs (assembleK, FEM.cpp:19-63,498-513).
-    p->launches += launchAssembleCoarse(p->stream, dc.g, dc.E, dFreeNode, p->ke.Ke, hc.scale, p->Kinv64, n);
+    // Kc = 2^(L-1+skip) sum_e E_e Ke on the free DOFs (assembleK, FEM.cpp:19-63,498-513),
+    // and the same with the volume-averaged modulus for the multiplicative cycle.
+    vfem_status st = invertCoarse(p, dFreeNode, dc.E, hc.scale, p->Kinv64, p->Kinv32);
+    if (st == VFEM_OK) st = invertCoarse(p, dFreeNode, dc.Ev, hc.scale, p->KinvV64, p->KinvV32);
+    cudaFree(dFreeNode);
+    return st;
+}
+
+// Dense Cholesky (cuSOLVER potrf) and inverse (potri) of scale * sum_e E_e Ke on
+// the coarsest free DOFs, symmetrised, with an FP32 copy.
+vfem_status invertCoarse(vfem_problem* p, const int32_t* dFreeNode, const float* E, double scale, double* K64,
+                         float* K32) {
+    DevLevel& dc = p->L.back();
+    const int64_t n = p->nc;
+    p->launches += launchAssembleCoarse(p->stream, dc.g, E, dFreeNode, p->ke.Ke, scale, K64, n);
     CK(cudaGetLastError());
     cusolverDnHandle_t h = nullptr;
-    if (cusolverDnCreate(&h) != CUSOLVER_STATUS_SUCCESS) {
-        cudaFree(dFreeNode);
-        return fail(VFEM_ERR_CUDA, "cusolverDnCreate failed");
-    }
+    if (cusolverDnCreate(&h) != CUSOLVER_STATUS_SUCCESS) return fail(VFEM_ERR_CUDA, "cusolverDnCreate failed");
     cusolverDnSetStream(h, p->stream);
     int lw1 = 0, lw2 = 0;
     vfem_status st = VFEM_OK;
     double* work = nullptr;
     int* info = nullptr;
     int hinfo = 0;
-    if (cusolverDnDpotrf_bufferSize(h, CUBLAS_FILL_MODE_LOWER, (int)n, p->Kinv64, (int)n, &lw1) !=
+    if (cusolverDnDpotrf_bufferSize(h, CUBLAS_FILL_MODE_LOWER, (int)n, K64, (int)n, &lw1) !=
             CUSOLVER_STATUS_SUCCESS ||
-        cusolverDnDpotri_bufferSize(h, CUBLAS_FILL_MODE_LOWER, (int)n, p->Kinv64, (int)n, &lw2) !=
+        cusolverDnDpotri_bufferSize(h, CUBLAS_FILL_MODE_LOWER, (int)n, K64, (int)n, &lw2) !=
             CUSOLVER_STATUS_SUCCESS) {
         st = fail(VFEM_ERR_CUDA, "cusolver buffer size query failed");
     }
@@ -193,7 +213,7 @@ vfem_status buildCoarse(vfem_problem* p) {
                           cudaMalloc(&info, sizeof(int)) != cudaSuccess))
         st = fail(VFEM_ERR_OUT_OF_MEMORY, "cusolver workspace");
     if (st == VFEM_OK) {
-        if (cusolverDnDpotrf(h, CUBLAS_FILL_MODE_LOWER, (int)n, p->Kinv64, (int)n, work, std::max(lw1, lw2), info) !=
+        if (cusolverDnDpotrf(h, CUBLAS_FILL_MODE_LOWER, (int)n, K64, (int)n, work, std::max(lw1, lw2), info) !=
             CUSOLVER_STATUS_SUCCESS)
             st = fail(VFEM_ERR_CUDA, "cusolverDnDpotrf failed");
         else {
@@ -204,7 +224,7 @@ vfem_status buildCoarse(vfem_problem* p) {
         }
     }
     if (st == VFEM_OK) {
-        if (cusolverDnDpotri(h, CUBLAS_FILL_MODE_LOWER, (int)n, p->Kinv64, (int)n, work, std::max(lw1, lw2), info) !=
+        if (cusolverDnDpotri(h, CUBLAS_FILL_MODE_LOWER, (int)n, K64, (int)n, work, std::max(lw1, lw2), info) !=
             CUSOLVER_STATUS_SUCCESS)
             st = fail(VFEM_ERR_CUDA, "cusolverDnDpotri failed");
         else {
@@ -215,13 +235,12 @@ vfem_status buildCoarse(vfem_problem* p) {
         }
     }
     if (st == VFEM_OK) {
-        p->launches += launchSymmetrizeLowerToFull(p->stream, p->Kinv64, n);
-        p->launches += launchConvert<double, float>(p->stream, n * n, p->Kinv64, p->Kinv32);
+        p->launches += launchSymmetrizeLowerToFull(p->stream, K64, n);
+        p->launches += launchConvert<double, float>(p->stream, n * n, K64, K32);
         if (cudaStreamSynchronize(p->stream) != cudaSuccess) st = fail(VFEM_ERR_CUDA, "coarse inverse kernels");
     }
     cudaFree(work);
     cudaFree(info);
-    cudaFree(dFreeNode);
     cusolverDnDestroy(h);
     return st;
 }
@@ -289,6 +308,8 @@ vfem_status createImpl(const uint8_t* vox, int nx, int ny, int nz, const double*
         d.nused = (int64_t)h.nodeStore.size();
         d.nelem = h.nelem;
         CKP(upload(&d.E, h.E));
+        if (i == 0) d.Ev = d.E;
+        else CKP(upload(&d.Ev, h.Ev));
         CKP(upload(&d.flags, h.flags));
         CKP(upload(&d.nodeStore, h.nodeStore));
         CKP(upload(&d.dinv64, h.dinv));
@@ -362,6 +383,12 @@ double* kinv<double>(vfem_problem* p) { return p->Kinv64; }
 template <>
 float* kinv<float>(vfem_problem* p) { return p->Kinv32; }
 template <typename T>
+T* kinvV(vfem_problem* p);
+template <>
+double* kinvV<double>(vfem_problem* p) { return p->KinvV64; }
+template <>
+float* kinvV<float>(vfem_problem* p) { return p->KinvV32; }
+template <typename T>
 T* cbuf(vfem_problem* p);
 template <>
 double* cbuf<double>(vfem_problem* p) { return p->cb64; }
@@ -400,7 +427,8 @@ int vcycle(vfem_problem* p, const vfem_options& o, int lv, T* r, T* z, T** outZ,
     LaunchCtx c = ctx(p);
     if (lv == L - 1) {
         // Coarsest: exact dense-inverse solve on the free DOFs; fixed and unused DOFs stay 0.
-        n += launchCoarseSolve<T>(c, kinv<T>(p), p->nc, p->freeDof, r, cbuf<T>(p), z, 1);
+        n += launchCoarseSolve<T>(c, o.mg_mode == VFEM_MG_VCYCLE ? kinvV<T>(p) : kinv<T>(p), p->nc, p->freeDof, r,
+                                  cbuf<T>(p), z, 1);
         if (lv == 0 && epi != EPI_NONE) n += launchDots<T>(c, l.nvec(), r, z, aux ? z : nullptr, aux, epi, 1);
         *outZ = z;
         return n;
@@ -423,6 +451,7 @@ int vcycle(vfem_problem* p, const vfem_options& o, int lv, T* r, T* z, T** outZ,
     n += launchJacobiZero<T>(c, l.g, r, dinv, l.flags, cur, o.omega, 1);
     for (int s = 1; s < o.pre_sweeps; ++s) {
         MatvecArgs<T> a = mvArgs<T>(p, lv, cur, other, MV_SMOOTH);
+        a.E = l.Ev;
         a.f = r;
         a.dinv = dinv;
         a.omega = o.omega;
@@ -431,6 +460,7 @@ int vcycle(vfem_problem* p, const vfem_options& o, int lv, T* r, T* z, T** outZ,
     }
     {
         MatvecArgs<T> a = mvArgs<T>(p, lv, cur, other, MV_RESID0);
+        a.E = l.Ev;
         a.f = r;
         n += matvec<T>(p, a);
     }
@@ -440,6 +470,7 @@ int vcycle(vfem_problem* p, const vfem_options& o, int lv, T* r, T* z, T** outZ,
     n += launchProlongAdd<T>(c, l.g, lc.g, lc.div, zc, l.flags, cur, 1);
     for (int s = 0; s < o.post_sweeps; ++s) {
         MatvecArgs<T> a = mvArgs<T>(p, lv, cur, other, MV_SMOOTH);
+        a.E = l.Ev;
         a.f = r;
         a.dinv = dinv;
         a.omega = o.omega;

@@ -186,14 +186,14 @@ void invert(std::vector<double>& d, const std::vector<uint8_t>& flags) {
         }
 }
 
-// Diagonal of scale * sum_e E_e Ke over the elements touching each node.
-void rediscretisedDiag(const HostLevel& l, const KeData& ke, std::vector<double>& d) {
+// Diagonal of scale * sum_e Ef_e Ke over the elements touching each node.
+void rediscretisedDiag(const HostLevel& l, const std::vector<float>& Ef, const KeData& ke, std::vector<double>& d) {
     const Grid& g = l.g;
     d.assign(3 * g.nnode, 0.0);
     for (int z = 0; z < g.ez; ++z)
         for (int y = 0; y < g.ey; ++y)
             for (int x = 0; x < g.ex; ++x) {
-                float E = l.E[g.store(x, y, z)];
+                float E = Ef[g.store(x, y, z)];
                 if (E == 0.f) continue;
                 for (int a = 0; a < 8; ++a) {
                     int64_t s = g.store(x + (a & 1), y + ((a >> 1) & 1), z + (a >> 2));
@@ -255,7 +255,8 @@ vfem_status buildHierarchy(const uint8_t* vox, int nx, int ny, int nz, const flo
         l0.flags[l0.nodeStore[fixed[i]]] |= FLAG_FIXED;
     }
     fixedIdsFromFlags(l0);
-    rediscretisedDiag(l0, ke, l0.dinv);
+    l0.Ev = l0.E;
+    rediscretisedDiag(l0, l0.E, ke, l0.dinv);
     l0.dinvRedisc = l0.dinv;
     invert(l0.dinv, l0.flags);
     invert(l0.dinvRedisc, l0.flags);
@@ -275,12 +276,13 @@ vfem_status buildHierarchy(const uint8_t* vox, int nx, int ny, int nz, const flo
         const std::vector<double>& tab = div == 4 ? tab4 : tab2;
         double childScale = std::pow(2.0, i - 1);
         c.E.assign(c.g.nnode, 0.f);
+        c.Ev.assign(c.g.nnode, 0.f);
         c.dinv.assign(3 * c.g.nnode, 0.0);
         // Coarse elements: used children, mean modulus, diagonal contributions.
         for (int z = 0; z < c.g.ez; ++z)
             for (int y = 0; y < c.g.ey; ++y)
                 for (int x = 0; x < c.g.ex; ++x) {
-                    double sumE = 0;
+                    double sumE = 0, sumEv = 0;
                     int cnt = 0;
                     double part[24] = {};
                     for (int ch = 0; ch < nch; ++ch) {
@@ -290,11 +292,13 @@ vfem_status buildHierarchy(const uint8_t* vox, int nx, int ny, int nz, const flo
                         if (Ef == 0.f) continue;
                         ++cnt;
                         sumE += Ef;
+                        sumEv += f.Ev[f.g.store(fx, fy, fz)];
                         for (int k = 0; k < 24; ++k) part[k] += childScale * (double)Ef * tab[(size_t)ch * 24 + k];
                     }
                     if (!cnt) continue;
                     float Ec = (float)(sumE / cnt);
                     c.E[c.g.store(x, y, z)] = Ec;
+                    c.Ev[c.g.store(x, y, z)] = (float)(sumEv / nch);
                     bool full = cnt == nch;
                     for (int a = 0; a < 8; ++a) {
                         int64_t s = c.g.store(x + (a & 1), y + ((a >> 1) & 1), z + (a >> 2));
@@ -321,7 +325,7 @@ vfem_status buildHierarchy(const uint8_t* vox, int nx, int ny, int nz, const flo
                     if (fx_) c.flags[c.g.store(x, y, z)] |= FLAG_FIXED;
                 }
         fixedIdsFromFlags(c);
-        rediscretisedDiag(c, ke, c.dinvRedisc);
+        rediscretisedDiag(c, c.Ev, ke, c.dinvRedisc);
         invert(c.dinv, c.flags);
         invert(c.dinvRedisc, c.flags);
         H.L.push_back(std::move(c));

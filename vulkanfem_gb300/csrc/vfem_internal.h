@@ -53,6 +53,8 @@ struct HostLevel {
     int divider = 2;               // coarsening factor from the previous level
     double scale = 1.0;            // operator multiplier 2^(level+skip)
     std::vector<float> E;          // per element (lower-corner storage index), 0 = empty
+    std::vector<float> Ev;         // multiplicative-cycle modulus: volume average of the children
+                                   // (empty children count as 0); equals E on the finest level
     std::vector<uint8_t> flags;    // per node
     std::vector<double> dinv;      // 3 per node: reference inverse diagonal (Galerkin for partial elements)
     std::vector<double> dinvRedisc;// 3 per node: inverse diagonal of the rediscretised operator

@@ -1,0 +1,138 @@
+"""Train the warm-start U-Net on solutions of the library's own solver and
+evaluate what it saves on unseen domains.
+
+    python -m vulkanfem_gb300.train_warmstart --samples 2000 --epochs 10 \
+        --out vulkanfem_gb300/checkpoints/unet_warmstart.npz --eval 8 --eval-n 128
+
+Training domains: 64^3 seeded random fields at 30-60% fill, a random load patch
+of total magnitude U[0.1, 1] in -z on the top face, z=0 fixed
+(``domains.training_field``); targets are the mixed-precision MG-PCG solutions
+(rtol 1e-6).  Evaluation: unseen seeds, cold start vs network warm start, both
+solved to the same FP64 relative residual; prints one JSON line.
+"""
+import argparse
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+from . import api, domains, learned
+
+NF = 9  # feature channels in use (see learned.py)
+
+def build_dataset(count, n, seed0, levels, log):
+    ke = domains.hex8_stiffness()
+    npad = learned.padded(n + 1)
+    F = np.zeros((count, npad, npad, npad, NF), np.float16)
+    T = np.zeros((count, npad, npad, npad, 3), np.float16)
+    M = np.zeros((count, npad, npad, npad), np.uint8)
+    t0 = time.time()
+    its = []
+    for i in range(count):
+        d = domains.training_field(n, seed=seed0 + i, levels=levels)
+        A = api.assembleSystemMatrix(d.voxels, ke, d.fixed, levels)
+        f = d.load_vector()
+        u, st = A.solve(f, precision="mixed")
+        its.append(st["iterations"])
+        feats, mask, scale = learned.domain_features(d, npad, A, f)
+        A.close()
+        F[i] = feats[..., :NF]
+        T[i] = learned.target_grid(u, mask, scale, npad)
+        M[i] = learned.loss_mask(mask, d.fixed, npad) > 0
+        if (i + 1) % 100 == 0:
+            log("data %d/%d  %.0f s  mean iterations %.1f" % (i + 1, count, time.time() - t0, np.mean(its)))
+    return F, T, M
+
+
+def expand(F, T, M, idx):
+    b = len(idx)
+    x = np.zeros((b,) + F.shape[1:4] + (learned.NCH,), np.float32)
+    x[..., :NF] = F[idx]
+    return x, T[idx].astype(np.float32), M[idx].astype(np.float32)
+
+
+def evaluate(params, count, n, seed0, levels, log):
+    ke = domains.hex8_stiffness()
+    net = learned.UNet(learned.padded(n + 1), params)
+    rows = []
+    for i in range(count):
+        d = domains.training_field(n, seed=seed0 + i, levels=levels)
+        A = api.assembleSystemMatrix(d.voxels, ke, d.fixed, levels)
+        f = d.load_vector()
+        A.solve(f, precision="mixed")  # graph capture outside the timing
+        _, cold = A.solve(f, precision="mixed")
+        t = time.perf_counter()
+        u0 = learned.warm_start(net, d, A, f)
+        t_pred = time.perf_counter() - t
+        _, warm = A.solve(f, u0=u0, precision="mixed")
+        feats = learned.domain_features(d, net.n, A, f)[0]
+        net.forward(feats)
+        t = time.perf_counter()
+        net.forward(feats)
+        t_fwd = time.perf_counter() - t
+        rows.append({"forward_ms": 1e3 * t_fwd,"cold_it": cold["iterations"], "warm_it": warm["iterations"],
+                     "cold_ms": cold["solve_ms"], "warm_ms": warm["solve_ms"], "predict_ms": 1e3 * t_pred,
+                     "cold_relres": cold["rel_residual"], "warm_relres": warm["rel_residual"]})
+        A.close()
+        log("eval %d: cold %d it %.1f ms, warm %d it %.1f ms (+%.1f ms predict)" % (
+            i, cold["iterations"], cold["solve_ms"], warm["iterations"], warm["solve_ms"], 1e3 * t_pred))
+    net.close()
+    return rows
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--samples", type=int, default=2000)
+    ap.add_argument("--n", type=int, default=64)
+    ap.add_argument("--levels", type=int, default=4)
+    ap.add_argument("--epochs", type=int, default=10)
+    ap.add_argument("--batch", type=int, default=4)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--out", default=learned.CHECKPOINT)
+    ap.add_argument("--eval", type=int, default=8)
+    ap.add_argument("--eval-n", type=int, default=128)
+    ap.add_argument("--eval-levels", type=int, default=5)
+    args = ap.parse_args(argv)
+    log = lambda s: print(s, file=sys.stderr, flush=True)
+    t0 = time.time()
+    F, T, M = build_dataset(args.samples, args.n, 0, args.levels, log)
+    t_data = time.time() - t0
+    net = learned.UNet(F.shape[1])
+    rng = np.random.default_rng(0)
+    hist = []
+    t1 = time.time()
+    for ep in range(args.epochs):
+        lr = args.lr * (0.5 ** (ep // max(1, args.epochs // 3)))
+        order = rng.permutation(args.samples)
+        losses = []
+        for s in range(0, args.samples - args.batch + 1, args.batch):
+            x, t, m = expand(F, T, M, order[s:s + args.batch])
+            losses.append(net.train_batch(x, t, m, lr)[0])
+        hist.append(float(np.mean(losses)))
+        log("epoch %d lr %.2e loss %.5f (%.0f s)" % (ep, lr, hist[-1], time.time() - t1))
+    t_train = time.time() - t1
+    params = net.get_params()
+    net.close()
+    if os.path.dirname(args.out):
+        os.makedirs(os.path.dirname(args.out), exist_ok=True)
+    learned.save(args.out, params, {"samples": args.samples, "epochs": args.epochs, "n": args.n,
+                                     "loss_history": np.asarray(hist)})
+    rows = evaluate(learned.load(args.out), args.eval, args.eval_n, 1_000_000, args.eval_levels, log)
+    summary = {
+        "samples": args.samples, "n": args.n, "epochs": args.epochs, "data_s": t_data, "train_s": t_train,
+        "loss_history": hist,
+        "eval_n": args.eval_n, "eval_count": len(rows),
+        "mean_cold_iterations": float(np.mean([r["cold_it"] for r in rows])),
+        "mean_warm_iterations": float(np.mean([r["warm_it"] for r in rows])),
+        "mean_cold_ms": float(np.mean([r["cold_ms"] for r in rows])),
+        "mean_warm_ms_incl_predict": float(np.mean([r["warm_ms"] + r["predict_ms"] for r in rows])),
+        "max_warm_relres": float(max(r["warm_relres"] for r in rows)),
+        "rows": rows,
+    }
+    print(json.dumps(summary), flush=True)
+
+
+if __name__ == "__main__":
+    main()
