@@ -415,6 +415,11 @@ int matvec(vfem_problem* p, const MatvecArgs<T>& a) {
     return launchMatvec<T>(ctx(p), a, p->ke.structured, opc<T>(p));
 }
 
+// FP64 vectors, double-float arithmetic (the mixed solve's true residual).
+int matvecDF(vfem_problem* p, const MatvecArgs<double>& a) {
+    return launchMatvecDF(ctx(p), a, p->ke.structured, p->op64);
+}
+
 // z = M^-1 r on level `lv` (r, z given); returns kernels; on level 0 the final
 // pass produces r.z (and z.aux) with epilogue `epi`.  *outZ receives the buffer
 // holding the result (it differs from z in the multiplicative cycle when the
@@ -526,13 +531,15 @@ int iteration(vfem_problem* p, const vfem_options& o, double** zOut64, float** z
         k += matvec<float>(p, a);
         k += launchUpdateXR<float, float>(c, n, p->x32, l0.r32, p->p32, p->Ap32);
         k += launchFlushX(c, n, p->x64, p->x32, 1);
-        MatvecArgs<double> t = mvArgs<double>(p, 0, p->x64, l0.r64, MV_RESID);
+        // True residual f - K x64 in double-float; only its FP32 rounding (the new
+        // recursive residual) and its norm are kept.
+        MatvecArgs<double> t = mvArgs<double>(p, 0, p->x64, nullptr, MV_RESID);
         t.f = p->f64;
         t.y32 = l0.r32;
         t.dot0 = DOT_OUT_OUT;
         t.epi = EPI_TRUE;
         t.condTrue = 1;
-        k += matvec<double>(p, t);
+        k += matvecDF(p, t);
         float* z = nullptr;
         k += precondition<float>(p, o, l0.r32, l0.z32, &z, o.flexible ? p->Ap32 : nullptr, EPI_BETA);
         k += launchUpdateP<float>(c, n, p->p32, z, 0);
@@ -575,8 +582,12 @@ vfem_status solveImpl(vfem_problem* p, const vfem_options* optIn, bool haveX0, v
         MatvecArgs<double> a = mvArgs<double>(p, 0, p->x64, l0.r64, MV_RESID);
         a.f = p->f64;
         a.checkDone = 0;
-        if (mixed) a.y32 = l0.r32;
-        launches += matvec<double>(p, a);
+        if (mixed) {
+            a.y32 = l0.r32;
+            launches += matvecDF(p, a);
+        } else {
+            launches += matvec<double>(p, a);
+        }
     } else {
         launches += launchFill<double>(p->stream, n, p->x64, 0.0);
         launches += launchConvert<double, double>(p->stream, n, p->f64, l0.r64);
@@ -945,9 +956,17 @@ vfem_status vfem_profile_kernels(vfem_problem* p, int32_t reps, double* ms) {
                     DevLevel& lc = p->L.back();
                     return launchCoarseSolve<double>(c, p->Kinv64, p->nc, p->freeDof, lc.r64, p->cb64, lc.z64, 1);
                 }
-                default: {
+                case VFEM_K_COARSE_FP32: {
                     DevLevel& lc = p->L.back();
                     return launchCoarseSolve<float>(c, p->Kinv32, p->nc, p->freeDof, lc.r32, p->cb32, lc.z32, 1);
+                }
+                default: {
+                    MatvecArgs<double> a = mvArgs<double>(p, 0, p->x64, nullptr, MV_RESID);
+                    a.f = p->f64;
+                    a.y32 = l0.t32;
+                    a.dot0 = DOT_OUT_OUT;
+                    a.epi = EPI_STORE;
+                    return matvecDF(p, a);
                 }
             }
         };

@@ -18,6 +18,7 @@
 #include <cfloat>
 #include <cstdio>
 #include <mutex>
+#include <type_traits>
 
 #include "kernels.h"
 
@@ -174,6 +175,87 @@ struct DotAcc<float> {
     __device__ __forceinline__ double get() const { return (double)s - (double)c; }
 };
 
+// Double-float ("df") numbers: the unevaluated sum hi + lo of two FP32 values,
+// about 48 significant bits, computed with FP32 instructions only (Dekker 1971:
+// TwoSum / FastTwoSum; the product error from one FMA).  GB300 issues FP64 at
+// about 1/64 of its FP32 rate, so the mixed-precision solve evaluates its true
+// residual f - K x in df: relative rounding ~1e-14 of the summed magnitudes,
+// several times faster than the FP64 product.  Addition is the "sloppy" variant
+// (error bounded by ~2^-44 (|a| + |b|)), ample for a residual that is compared
+// with 1e-6 |f|.  The compiler must not re-associate these expressions, which
+// nvcc does not do without fast-math flags.
+struct df {
+    float hi, lo;
+    df() = default;
+    __host__ __device__ constexpr df(float h, float l) : hi(h), lo(l) {}
+    __host__ __device__ constexpr explicit df(int v) : hi((float)v), lo(0.f) {}
+    __host__ __device__ constexpr explicit df(float v) : hi(v), lo(0.f) {}
+    __host__ __device__ explicit df(double v) : hi((float)v), lo((float)(v - (double)(float)v)) {}
+};
+
+__device__ __forceinline__ df dfTwoSum(float a, float b) {
+    const float s = a + b;
+    const float bb = s - a;
+    return df(s, (a - (s - bb)) + (b - bb));
+}
+__device__ __forceinline__ df dfFastTwoSum(float a, float b) {  // |a| >= |b|
+    const float s = a + b;
+    return df(s, b - (s - a));
+}
+__device__ __forceinline__ df operator+(df a, df b) {
+    const df s = dfTwoSum(a.hi, b.hi);
+    return dfFastTwoSum(s.hi, s.lo + (a.lo + b.lo));
+}
+__device__ __forceinline__ df operator-(df a, df b) { return a + df(-b.hi, -b.lo); }
+__device__ __forceinline__ df operator*(df a, df b) {
+    const float p = a.hi * b.hi;
+    float e = fmaf(a.hi, b.hi, -p);
+    e = fmaf(a.hi, b.lo, e);
+    e = fmaf(a.lo, b.hi, e);
+    return dfFastTwoSum(p, e);
+}
+__device__ __forceinline__ df& operator+=(df& a, df b) { return a = a + b; }
+__device__ __forceinline__ df& operator*=(df& a, df b) { return a = a * b; }
+// The df overload below would hide the global fma from unqualified calls in
+// this namespace; these restore the FP32 and FP64 forms.
+__device__ __forceinline__ float fma(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double fma(double a, double b, double c) { return ::fma(a, b, c); }
+// a * b + c with one renormalisation.
+__device__ __forceinline__ df fma(df a, df b, df c) {
+    const float p = a.hi * b.hi;
+    const float pe = fmaf(a.hi, b.hi, -p);
+    const df s = dfTwoSum(p, c.hi);
+    float t = s.lo + (pe + c.lo);
+    t = fmaf(a.hi, b.lo, t);
+    t = fmaf(a.lo, b.hi, t);
+    return dfFastTwoSum(s.hi, t);
+}
+
+// Conversions between a storage type T and a compute type TC of the matvec.
+template <typename T, typename TC>
+struct Cvt {
+    static __device__ __forceinline__ TC in(T v) { return TC(v); }
+    static __device__ __forceinline__ T out(TC v) { return T(v); }
+};
+template <>
+struct Cvt<double, df> {
+    static __device__ __forceinline__ df in(double v) {
+        const float h = __double2float_rn(v);
+        return df(h, __double2float_rn(v - (double)h));
+    }
+    static __device__ __forceinline__ double out(df v) { return (double)v.hi + (double)v.lo; }
+};
+__device__ __forceinline__ float toF(float v) { return v; }
+__device__ __forceinline__ float toF(double v) { return (float)v; }
+__device__ __forceinline__ float toF(df v) { return v.hi; }  // hi is v rounded to FP32
+
+template <>
+struct DotAcc<df> {
+    df s = df(0.f, 0.f);
+    __device__ __forceinline__ void add(df v) { s = s + v; }
+    __device__ __forceinline__ double get() const { return (double)s.hi + (double)s.lo; }
+};
+
 template <typename T>
 struct Ks {
     T v[45];
@@ -205,11 +287,10 @@ __device__ __forceinline__ void fwht8x3(T (&v)[24]) {
 // y = e * Ke u for an isotropic cube element: Ke = H^T Khat H with Khat on the
 // 45-entry pattern (8 symmetry classes), H the per-component Walsh-Hadamard
 // transform.  ~190 flops instead of 1152 for the dense 24x24 product.
+// y = Khat u on the 45-entry pattern (modes 1..7; mode 0, the rigid translation,
+// has no energy).  u and y hold 3 m + c for mode m and component c.
 template <typename T>
-__device__ __forceinline__ void elemStruct(T (&u)[24], T (&y)[24], const Ks<T>& k, T e) {
-    fwht8x3(u);
-#pragma unroll
-    for (int i = 3; i < 24; ++i) u[i] *= e;
+__device__ __forceinline__ void applyKhat(const T (&u)[24], T (&y)[24], const Ks<T>& k) {
 #pragma unroll
     for (int i = 0; i < 24; ++i) y[i] = T(0);
 #define KS_(n, r, c) y[r] = fma(k.v[n], u[c], y[r]);
@@ -224,6 +305,14 @@ __device__ __forceinline__ void elemStruct(T (&u)[24], T (&y)[24], const Ks<T>& 
     KS_(36, 18, 18) KS_(37, 18, 16) KS_(38, 18, 11) KS_(39, 16, 18) KS_(40, 16, 16) KS_(41, 16, 11)
     KS_(42, 11, 18) KS_(43, 11, 16) KS_(44, 11, 11)
 #undef KS_
+}
+
+template <typename T>
+__device__ __forceinline__ void elemStruct(T (&u)[24], T (&y)[24], const Ks<T>& k, T e) {
+    fwht8x3(u);
+#pragma unroll
+    for (int i = 3; i < 24; ++i) u[i] *= e;
+    applyKhat<T>(u, y, k);
     fwht8x3(y);
 }
 
@@ -266,8 +355,20 @@ __device__ __forceinline__ void stSlot<double>(double* p, double a, double b, do
     reinterpret_cast<double2*>(p)[0] = make_double2(a, b);
     reinterpret_cast<double2*>(p)[1] = make_double2(c, 0.0);
 }
+template <>
+__device__ __forceinline__ void stSlot<df>(df* p, df a, df b, df c) {
+    reinterpret_cast<float4*>(p)[0] = make_float4(a.hi, a.lo, b.hi, b.lo);
+    reinterpret_cast<float4*>(p)[1] = make_float4(c.hi, c.lo, 0.f, 0.f);
+}
 template <typename T>
 __device__ __forceinline__ void ldSlot(const T* p, T& a, T& b, T& c);
+template <>
+__device__ __forceinline__ void ldSlot<df>(const df* p, df& a, df& b, df& c) {
+    const float4 v0 = reinterpret_cast<const float4*>(p)[0], v1 = reinterpret_cast<const float4*>(p)[1];
+    a = df(v0.x, v0.y);
+    b = df(v0.z, v0.w);
+    c = df(v1.x, v1.y);
+}
 template <>
 __device__ __forceinline__ void ldSlot<float>(const float* p, float& a, float& b, float& c) {
     const float4 v = *reinterpret_cast<const float4*>(p);
@@ -283,6 +384,35 @@ __device__ __forceinline__ void ldSlot<double>(const double* p, double& a, doubl
     c = v1.x;
 }
 
+// Output stage of the matvec kernels for one owned node s: sum = (K x)_s before
+// the fixed-row mask; writes y (and y32) by mode and accumulates the dots.
+template <typename T, typename TC>
+__device__ __forceinline__ void mvOutput(const MatvecArgs<T>& a, int64_t s, const TC (&sum)[3], bool fixed,
+                                         const TC (&xo)[3], DotAcc<TC>& d0, DotAcc<TC>& d1) {
+    typedef Cvt<T, TC> C;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const TC ax = fixed ? TC(0) : sum[c];
+        TC out;
+        TC fv = TC(0);
+        if (a.mode != MV_AX) fv = C::in(a.f[3 * s + c]);
+        const TC xv = xo[c];
+        switch (a.mode) {
+            case MV_AX: out = ax; break;
+            case MV_RESID: out = fv - ax; break;
+            case MV_RESID0: out = fixed ? TC(0) : fv - ax; break;
+            default: out = fixed ? TC(0) : xv + TC(a.omega) * C::in(a.dinv[3 * s + c]) * (fv - ax); break;
+        }
+        if constexpr (std::is_same<T, TC>::value) a.y[3 * s + c] = out;
+        else if (a.y) a.y[3 * s + c] = C::out(out);
+        if (a.y32) a.y32[3 * s + c] = toF(out);
+        if (a.dot0 == DOT_X_OUT) d0.add(xv * out);
+        else if (a.dot0 == DOT_OUT_OUT) d0.add(out * out);
+        else if (a.dot0 == DOT_F_OUT) d0.add(fv * out);
+        if (a.dot1) d1.add(out * C::in(a.aux[3 * s + c]));
+    }
+}
+
 // Element-by-element product on a 2.5-D tile.  A block of 32 x 8 threads marches
 // up a z-range; at each element layer thread (tx,ty) computes the element whose
 // lower corner is node (x0+tx-1, y0+ty-1) and owns node (x0+tx, y0+ty), which is
@@ -295,14 +425,18 @@ __device__ __forceinline__ void ldSlot<double>(const double* p, double& a, doubl
 // are already in flight to registers.  The 33 x 9 node tile of a layer is
 // loaded without integer division: every thread loads its own slot, row 8
 // comes from the ty == 0 threads and column 32 from nine threads of row 1.
-template <typename T, bool STRUCT>
-__global__ void __launch_bounds__(MV_TX* MV_TY, STRUCT ? (sizeof(T) == 4 ? 4 : 2) : 1)
-    kMatvec(MatvecArgs<T> a, const typename KP<T, STRUCT>::type kp, Scalars* S, RedBuf rb) {
+//
+// T is the storage type of the vectors, TC the arithmetic type (T, or df for
+// the true residual of the mixed-precision solve: FP64 vectors, df arithmetic).
+template <typename T, bool STRUCT, typename TC = T>
+__global__ void __launch_bounds__(MV_TX* MV_TY, STRUCT ? (sizeof(TC) == 4 ? 4 : 2) : 1)
+    kMatvec(MatvecArgs<T> a, const typename KP<TC, STRUCT>::type kp, Scalars* S, RedBuf rb) {
     if (a.checkDone && S->done) return;
     if (a.condTrue && !trueResidualDue(S)) return;
+    typedef Cvt<T, TC> C;
     extern __shared__ __align__(16) unsigned char smemRaw[];
-    T* su = reinterpret_cast<T*>(smemRaw);
-    T* sy = su + kSuElems;
+    TC* su = reinterpret_cast<TC*>(smemRaw);
+    TC* sy = su + kSuElems;
     const Grid g = a.g;
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int x0 = blockIdx.x * (MV_TX - 1), y0 = blockIdx.y * (MV_TY - 1), z0 = blockIdx.z * MV_ZC;
@@ -314,7 +448,7 @@ __global__ void __launch_bounds__(MV_TX* MV_TY, STRUCT ? (sizeof(T) == 4 ? 4 : 2
     const bool ecxy = ecx >= 0 && ecx < g.ex && ecy >= 0 && ecy < g.ey;
     const int eCol = ecy * g.nx + ecx;   // in-plane offsets fit in 32 bits for every accepted grid
     const int oCol = ony * g.nx + onx;
-    const T sc = (T)a.scale;
+    const TC sc = TC(a.scale);
     // Extra tile slots: row MV_TY (ty == 0 threads), column MV_TX (row-1 threads tx <= MV_TY).
     const bool hasR = ty == 0, hasC = (ty == 1) && (tx <= MV_TY);
     const int rX = x0 - 1 + tx, rY = y0 - 1 + MV_TY;
@@ -345,9 +479,9 @@ __global__ void __launch_bounds__(MV_TX* MV_TY, STRUCT ? (sizeof(T) == 4 ? 4 : 2
     };
     auto sstore = [&](int zl) {
         const int b = zl & 1;
-        stSlot<T>(SU(b, ty, tx), pf[0], pf[1], pf[2]);
-        if (hasR) stSlot<T>(SU(b, MV_TY, tx), pf[3], pf[4], pf[5]);
-        if (hasC) stSlot<T>(SU(b, tx, MV_TX), pf[6], pf[7], pf[8]);
+        stSlot<TC>(SU(b, ty, tx), C::in(pf[0]), C::in(pf[1]), C::in(pf[2]));
+        if (hasR) stSlot<TC>(SU(b, MV_TY, tx), C::in(pf[3]), C::in(pf[4]), C::in(pf[5]));
+        if (hasC) stSlot<TC>(SU(b, tx, MV_TX), C::in(pf[6]), C::in(pf[7]), C::in(pf[8]));
     };
     auto eload = [&](int k) -> float {
         return (ecxy && k >= 0 && k < g.ez) ? a.E[(int64_t)eCol + (int64_t)k * plane] : 0.f;
@@ -355,8 +489,8 @@ __global__ void __launch_bounds__(MV_TX* MV_TY, STRUCT ? (sizeof(T) == 4 ? 4 : 2
     auto fload = [&](int k) -> uint8_t {
         return (owner && k >= z0 && k < zend) ? a.flags[(int64_t)oCol + (int64_t)k * plane] : (uint8_t)0;
     };
-    T acc[3] = {T(0), T(0), T(0)};
-    DotAcc<T> d0, d1;
+    TC acc[3] = {TC(0), TC(0), TC(0)};
+    DotAcc<TC> d0, d1;
     gload(z0 - 1);
     sstore(z0 - 1);
     gload(z0);
@@ -372,80 +506,241 @@ __global__ void __launch_bounds__(MV_TX* MV_TY, STRUCT ? (sizeof(T) == 4 ? 4 : 2
         flNext = fload(k + 1);
         // x at the owned node of layer k, read now: the next iteration's store
         // overwrites this layer's buffer without waiting for the output phase.
-        T xo[3];
-        ldSlot<T>(SU(k & 1, ty + 1, tx + 1), xo[0], xo[1], xo[2]);
-        T ye[24];
+        TC xo[3];
+        ldSlot<TC>(SU(k & 1, ty + 1, tx + 1), xo[0], xo[1], xo[2]);
+        TC ye[24];
         if (Ee != 0.f) {
-            T u[24];
+            TC u[24];
 #pragma unroll
             for (int n = 0; n < 8; ++n) {
                 const int dx = n & 1, dy = (n >> 1) & 1, dz = n >> 2;
-                ldSlot<T>(SU((k + dz) & 1, ty + dy, tx + dx), u[3 * n], u[3 * n + 1], u[3 * n + 2]);
+                ldSlot<TC>(SU((k + dz) & 1, ty + dy, tx + dx), u[3 * n], u[3 * n + 1], u[3 * n + 2]);
             }
-            if constexpr (STRUCT) elemStruct<T>(u, ye, kp, sc * (T)Ee);
-            else elemDense<T>(u, ye, kp, sc * (T)Ee);
+            if constexpr (STRUCT) elemStruct<TC>(u, ye, kp, sc * TC(Ee));
+            else elemDense<TC>(u, ye, kp, sc * TC(Ee));
         } else {
 #pragma unroll
-            for (int i = 0; i < 24; ++i) ye[i] = T(0);
+            for (int i = 0; i < 24; ++i) ye[i] = TC(0);
         }
-        stSlot<T>(SY(0, ty, tx), ye[0], ye[1], ye[2]);     // a = 0
-        stSlot<T>(SY(1, ty, tx), ye[3], ye[4], ye[5]);     // a = 1
-        stSlot<T>(SY(2, ty, tx), ye[6], ye[7], ye[8]);     // a = 2
-        stSlot<T>(SY(3, ty, tx), ye[12], ye[13], ye[14]);  // a = 4
-        stSlot<T>(SY(4, ty, tx), ye[15], ye[16], ye[17]);  // a = 5
-        stSlot<T>(SY(5, ty, tx), ye[18], ye[19], ye[20]);  // a = 6
+        stSlot<TC>(SY(0, ty, tx), ye[0], ye[1], ye[2]);     // a = 0
+        stSlot<TC>(SY(1, ty, tx), ye[3], ye[4], ye[5]);     // a = 1
+        stSlot<TC>(SY(2, ty, tx), ye[6], ye[7], ye[8]);     // a = 2
+        stSlot<TC>(SY(3, ty, tx), ye[12], ye[13], ye[14]);  // a = 4
+        stSlot<TC>(SY(4, ty, tx), ye[15], ye[16], ye[17]);  // a = 5
+        stSlot<TC>(SY(5, ty, tx), ye[18], ye[19], ye[20]);  // a = 6
         __syncthreads();
         if (owner) {
-            T lo[3], hi[3], q[3];
+            TC lo[3], hi[3], q[3];
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
                 lo[c] = ye[9 + c];
                 hi[c] = ye[21 + c];
             }
-            ldSlot<T>(SY(2, ty, tx + 1), q[0], q[1], q[2]);
+            ldSlot<TC>(SY(2, ty, tx + 1), q[0], q[1], q[2]);
 #pragma unroll
             for (int c = 0; c < 3; ++c) lo[c] += q[c];
-            ldSlot<T>(SY(1, ty + 1, tx), q[0], q[1], q[2]);
+            ldSlot<TC>(SY(1, ty + 1, tx), q[0], q[1], q[2]);
 #pragma unroll
             for (int c = 0; c < 3; ++c) lo[c] += q[c];
-            ldSlot<T>(SY(0, ty + 1, tx + 1), q[0], q[1], q[2]);
+            ldSlot<TC>(SY(0, ty + 1, tx + 1), q[0], q[1], q[2]);
 #pragma unroll
             for (int c = 0; c < 3; ++c) lo[c] += q[c];
-            ldSlot<T>(SY(5, ty, tx + 1), q[0], q[1], q[2]);
+            ldSlot<TC>(SY(5, ty, tx + 1), q[0], q[1], q[2]);
 #pragma unroll
             for (int c = 0; c < 3; ++c) hi[c] += q[c];
-            ldSlot<T>(SY(4, ty + 1, tx), q[0], q[1], q[2]);
+            ldSlot<TC>(SY(4, ty + 1, tx), q[0], q[1], q[2]);
 #pragma unroll
             for (int c = 0; c < 3; ++c) hi[c] += q[c];
-            ldSlot<T>(SY(3, ty + 1, tx + 1), q[0], q[1], q[2]);
+            ldSlot<TC>(SY(3, ty + 1, tx + 1), q[0], q[1], q[2]);
 #pragma unroll
             for (int c = 0; c < 3; ++c) hi[c] += q[c];
             if (k >= z0) {
-                const int64_t s = (int64_t)oCol + (int64_t)k * plane;
-                const bool fixed = (fl & FLAG_FIXED) != 0;
+                TC sum[3];
 #pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    const T ax = fixed ? T(0) : acc[c] + lo[c];
-                    T out;
-                    T fv = T(0);
-                    if (a.mode != MV_AX) fv = a.f[3 * s + c];
-                    const T xv = xo[c];
-                    switch (a.mode) {
-                        case MV_AX: out = ax; break;
-                        case MV_RESID: out = fv - ax; break;
-                        case MV_RESID0: out = fixed ? T(0) : fv - ax; break;
-                        default: out = fixed ? T(0) : xv + (T)a.omega * a.dinv[3 * s + c] * (fv - ax); break;
-                    }
-                    a.y[3 * s + c] = out;
-                    if (a.y32) a.y32[3 * s + c] = (float)out;
-                    if (a.dot0 == DOT_X_OUT) d0.add(xv * out);
-                    else if (a.dot0 == DOT_OUT_OUT) d0.add(out * out);
-                    else if (a.dot0 == DOT_F_OUT) d0.add(fv * out);
-                    if (a.dot1) d1.add(out * a.aux[3 * s + c]);
-                }
+                for (int c = 0; c < 3; ++c) sum[c] = acc[c] + lo[c];
+                mvOutput<T, TC>(a, (int64_t)oCol + (int64_t)k * plane, sum, (fl & FLAG_FIXED) != 0, xo, d0, d1);
             }
 #pragma unroll
             for (int c = 0; c < 3; ++c) acc[c] = hi[c];
+        }
+    }
+#undef SU
+#undef SY
+    if (a.epi != EPI_NONE) {
+        double v[2] = {d0.get(), d1.get()}, t[2];
+        if (gridReduce<MV_TX * MV_TY, 2>(v, rb, t)) applyEpi(a.epi, S, t[0], t[1]);
+    }
+}
+
+// 4-point Walsh-Hadamard transform of a node quad (corner q = dx + 2 dy), per
+// component: v[3m+c] = sum_q (-1)^popcount(m&q) u[3q+c].
+template <typename T>
+__device__ __forceinline__ void fwht4x3(T (&v)[12]) {
+#pragma unroll
+    for (int s = 1; s < 4; s <<= 1) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            if (q & s) continue;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const T p = v[3 * q + c], r = v[3 * (q + s) + c];
+                v[3 * q + c] = p + r;
+                v[3 * (q + s) + c] = p - r;
+            }
+        }
+    }
+}
+
+// The structured (isotropic cube) product with the Walsh-Hadamard factors
+// shared along z.  With corner a = (q, dz) and mode m = (mq, mz), the 8-point
+// transform splits into the 4-point transforms Q_0, Q_1 of the element's bottom
+// and top node quads: uh[(mq,0)] = Q_0 + Q_1, uh[(mq,1)] = Q_0 - Q_1.  The top
+// quad's transform of element layer k is the bottom one of layer k+1, so each
+// quad is transformed once.  On the way back the top-face output of layer k-1
+// and the bottom-face output of layer k land on the same node quad and are
+// added in the Walsh domain before one inverse 4-point transform.  Per element
+// this halves the shared-memory node reads (4 instead of 8), the exported
+// contributions (3 instead of 6) and the quad transforms, against kMatvec.
+// Same tile, pipelining and output stage as kMatvec.  The two Walsh-domain
+// carries stay in registers across the z march.  Launch bounds, measured on
+// the 256^3 workload: FP32 3 blocks per SM (80 registers, no spills; 4 blocks
+// spill and run 33% slower); FP64 and df 2 blocks per SM (128 registers, a few
+// spilled values; 20% faster than 1 block without spills).
+template <typename T, typename TC>
+__global__ void __launch_bounds__(MV_TX* MV_TY, sizeof(TC) == 4 ? 3 : 2)
+    kMatvecH(MatvecArgs<T> a, const Ks<TC> kp, Scalars* S, RedBuf rb) {
+    if (a.checkDone && S->done) return;
+    if (a.condTrue && !trueResidualDue(S)) return;
+    typedef Cvt<T, TC> C;
+    extern __shared__ __align__(16) unsigned char smemRaw[];
+    TC* su = reinterpret_cast<TC*>(smemRaw);
+    TC* sy = su + kSuElems;
+    const Grid g = a.g;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int x0 = blockIdx.x * (MV_TX - 1), y0 = blockIdx.y * (MV_TY - 1), z0 = blockIdx.z * MV_ZC;
+    const int zend = min(z0 + MV_ZC, g.nz);
+    const int64_t plane = (int64_t)g.nx * g.ny;
+    const int ecx = x0 + tx - 1, ecy = y0 + ty - 1;
+    const int onx = x0 + tx, ony = y0 + ty;
+    const bool owner = (tx < MV_TX - 1) && (ty < MV_TY - 1) && onx < g.nx && ony < g.ny;
+    const bool ecxy = ecx >= 0 && ecx < g.ex && ecy >= 0 && ecy < g.ey;
+    const int eCol = ecy * g.nx + ecx;
+    const int oCol = ony * g.nx + onx;
+    const TC sc = TC(a.scale);
+    const bool hasR = ty == 0, hasC = (ty == 1) && (tx <= MV_TY);
+    const int rX = x0 - 1 + tx, rY = y0 - 1 + MV_TY;
+    const int cX = x0 - 1 + MV_TX, cY = y0 - 1 + tx;
+    const bool ok0 = ecx >= 0 && ecx < g.nx && ecy >= 0 && ecy < g.ny;
+    const bool okR = hasR && rX >= 0 && rX < g.nx && rY >= 0 && rY < g.ny;
+    const bool okC = hasC && cX >= 0 && cX < g.nx && cY >= 0 && cY < g.ny;
+#define SU(b, iy, ix) (su + (((((b) * (MV_TY + 1)) + (iy)) * (MV_TX + 1) + (ix)) << 2))
+#define SY(k, iy, ix) (sy + (((((k) * MV_TY) + (iy)) * MV_TX + (ix)) << 2))
+    T pf[9];
+    auto gload = [&](int zl) {
+        const bool zok = zl >= 0 && zl < g.nz;
+        const int64_t zoff = (int64_t)zl * plane;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) pf[i] = T(0);
+        if (ok0 && zok) {
+            const T* p = a.x + 3 * ((int64_t)eCol + zoff);
+            pf[0] = p[0]; pf[1] = p[1]; pf[2] = p[2];
+        }
+        if (okR && zok) {
+            const T* p = a.x + 3 * ((int64_t)(rY * g.nx + rX) + zoff);
+            pf[3] = p[0]; pf[4] = p[1]; pf[5] = p[2];
+        }
+        if (okC && zok) {
+            const T* p = a.x + 3 * ((int64_t)(cY * g.nx + cX) + zoff);
+            pf[6] = p[0]; pf[7] = p[1]; pf[8] = p[2];
+        }
+    };
+    auto sstore = [&](int zl) {
+        const int b = zl & 1;
+        stSlot<TC>(SU(b, ty, tx), C::in(pf[0]), C::in(pf[1]), C::in(pf[2]));
+        if (hasR) stSlot<TC>(SU(b, MV_TY, tx), C::in(pf[3]), C::in(pf[4]), C::in(pf[5]));
+        if (hasC) stSlot<TC>(SU(b, tx, MV_TX), C::in(pf[6]), C::in(pf[7]), C::in(pf[8]));
+    };
+    auto eload = [&](int k) -> float {
+        return (ecxy && k >= 0 && k < g.ez) ? a.E[(int64_t)eCol + (int64_t)k * plane] : 0.f;
+    };
+    auto fload = [&](int k) -> uint8_t {
+        return (owner && k >= z0 && k < zend) ? a.flags[(int64_t)oCol + (int64_t)k * plane] : (uint8_t)0;
+    };
+    // Walsh-domain quad of the current bottom node layer, and the top-face
+    // output of the previous element layer (Walsh domain).
+    TC qb[12], carry[12];
+#pragma unroll
+    for (int i = 0; i < 12; ++i) carry[i] = TC(0);
+    DotAcc<TC> d0, d1;
+    gload(z0 - 1);
+    sstore(z0 - 1);
+    gload(z0);
+    float Enext = eload(z0 - 1);
+    uint8_t flNext = fload(z0 - 1);
+    for (int k = z0 - 1; k < zend; ++k) {
+        sstore(k + 1);
+        const float Ee = Enext;
+        const uint8_t fl = flNext;
+        __syncthreads();
+        gload(k + 2);
+        Enext = eload(k + 1);
+        flNext = fload(k + 1);
+        TC xo[3];
+        ldSlot<TC>(SU(k & 1, ty + 1, tx + 1), xo[0], xo[1], xo[2]);
+        if (k == z0 - 1) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                ldSlot<TC>(SU(k & 1, ty + (q >> 1), tx + (q & 1)), qb[3 * q], qb[3 * q + 1], qb[3 * q + 2]);
+            fwht4x3<TC>(qb);
+        }
+        TC qt[12];
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            ldSlot<TC>(SU((k + 1) & 1, ty + (q >> 1), tx + (q & 1)), qt[3 * q], qt[3 * q + 1], qt[3 * q + 2]);
+        fwht4x3<TC>(qt);
+        TC nb[12];  // node layer k: Walsh-domain contributions at the element's bottom quad
+        if (Ee != 0.f) {
+            TC uh[24], yh[24];
+            const TC e = sc * TC(Ee);
+#pragma unroll
+            for (int i = 0; i < 12; ++i) {
+                uh[i] = qb[i] + qt[i];
+                uh[12 + i] = qb[i] - qt[i];
+            }
+#pragma unroll
+            for (int i = 3; i < 24; ++i) uh[i] *= e;
+            applyKhat<TC>(uh, yh, kp);
+#pragma unroll
+            for (int i = 0; i < 12; ++i) {
+                nb[i] = carry[i] + (yh[i] + yh[12 + i]);
+                carry[i] = yh[i] - yh[12 + i];
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < 12; ++i) {
+                nb[i] = carry[i];
+                carry[i] = TC(0);
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < 12; ++i) qb[i] = qt[i];
+        fwht4x3<TC>(nb);
+        stSlot<TC>(SY(0, ty, tx), nb[0], nb[1], nb[2]);  // corner (0,0)
+        stSlot<TC>(SY(1, ty, tx), nb[3], nb[4], nb[5]);  // corner (1,0)
+        stSlot<TC>(SY(2, ty, tx), nb[6], nb[7], nb[8]);  // corner (0,1)
+        __syncthreads();
+        if (owner && k >= z0) {
+            TC sum[3] = {nb[9], nb[10], nb[11]}, q[3];  // own corner (1,1)
+            ldSlot<TC>(SY(2, ty, tx + 1), q[0], q[1], q[2]);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) sum[c] += q[c];
+            ldSlot<TC>(SY(1, ty + 1, tx), q[0], q[1], q[2]);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) sum[c] += q[c];
+            ldSlot<TC>(SY(0, ty + 1, tx + 1), q[0], q[1], q[2]);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) sum[c] += q[c];
+            mvOutput<T, TC>(a, (int64_t)oCol + (int64_t)k * plane, sum, (fl & FLAG_FIXED) != 0, xo, d0, d1);
         }
     }
 #undef SU
@@ -502,6 +797,73 @@ __global__ void __launch_bounds__(256) kRestrict(Grid gf, Grid gc, const T* __re
 }
 
 // Trilinear prolongation of coarse node values to fine node (fx,fy,fz).
+// The same full weighting for the 2x coarsening, separably and with reuse:
+// a thread owns coarse column (cx, cy) and marches PZC coarse layers up z.
+// rc(cz) = P(2cz-1)/2 + P(2cz) + P(2cz+1)/2 with the fine-plane sums
+// P(fz) = sum_dy w_dy (r(2cx-1)/2 + r(2cx) + r(2cx+1)/2) at row 2cy+dy; P(2cz+1)
+// is kept for the next layer, and r(2cx-1) of a lane is r(2cx+1) of the lane
+// below (a warp shuffle), so each fine value is loaded about 1.5 times.
+constexpr int PZR = 4;
+template <typename T>
+__global__ void __launch_bounds__(256) kRestrict2(Grid gf, Grid gc, const T* __restrict__ rf, T* __restrict__ rc,
+                                                  const Scalars* S, int checkDone) {
+    if (checkDone && S->done) return;
+    const int lane = threadIdx.x;
+    const int cx = blockIdx.x * 32 + lane, cy = blockIdx.y * 8 + threadIdx.y;
+    const bool valid = cx < gc.nx && cy < gc.ny;
+    const T half = T(0.5);
+    const int fx0 = 2 * cx;
+    // Weighted row sum at fine row fy of layer fz into s[3]; all lanes take part
+    // (shuffles), out-of-grid fine nodes count 0.
+    auto rowSum = [&](int fy, int fz, T (&s)[3]) {
+        const bool rowOk = fy >= 0 && fy < gf.ny && fz >= 0 && fz < gf.nz;
+        const int64_t base = rowOk ? gf.store(0, fy, fz) : 0;
+        T c0[3] = {T(0), T(0), T(0)}, c1[3] = {T(0), T(0), T(0)}, cm[3] = {T(0), T(0), T(0)};
+        if (rowOk && fx0 < gf.nx) {
+            const T* p = rf + 3 * (base + fx0);
+            c0[0] = p[0]; c0[1] = p[1]; c0[2] = p[2];
+        }
+        if (rowOk && fx0 + 1 < gf.nx) {
+            const T* p = rf + 3 * (base + fx0 + 1);
+            c1[0] = p[0]; c1[1] = p[1]; c1[2] = p[2];
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) cm[c] = __shfl_up_sync(0xffffffffu, c1[c], 1);
+        if (lane == 0) {
+            cm[0] = cm[1] = cm[2] = T(0);
+            if (rowOk && fx0 - 1 >= 0 && fx0 - 1 < gf.nx) {
+                const T* p = rf + 3 * (base + fx0 - 1);
+                cm[0] = p[0]; cm[1] = p[1]; cm[2] = p[2];
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) s[c] = c0[c] + half * (cm[c] + c1[c]);
+    };
+    auto planeSum = [&](int fz, T (&P)[3]) {
+        T a[3], b[3], d[3];
+        rowSum(2 * cy - 1, fz, a);
+        rowSum(2 * cy, fz, b);
+        rowSum(2 * cy + 1, fz, d);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) P[c] = b[c] + half * (a[c] + d[c]);
+    };
+    const int cz0 = blockIdx.z * PZR, cz1 = min(gc.nz, cz0 + PZR);
+    T Pm[3];
+    planeSum(2 * cz0 - 1, Pm);
+    for (int cz = cz0; cz < cz1; ++cz) {
+        T P0[3], Pp[3];
+        planeSum(2 * cz, P0);
+        planeSum(2 * cz + 1, Pp);
+        if (valid) {
+            T* q = rc + 3 * gc.store(cx, cy, cz);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) q[c] = P0[c] + half * (Pm[c] + Pp[c]);
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) Pm[c] = Pp[c];
+    }
+}
+
 template <typename T, int DIV>
 __device__ __forceinline__ void prolongAt(const Grid& gf, const Grid& gc, const T* zc, int fx, int fy, int fz,
                                           T (&acc)[3]) {
@@ -567,6 +929,105 @@ __global__ void __launch_bounds__(256)
                     d0.add(r[c] * out[c]);
                     if (aux) d1.add(out[c] * aux[3 * s + c]);
                 }
+            }
+        }
+    }
+    if (epi != EPI_NONE) {
+        double v[2] = {d0.get(), d1.get()}, t[2];
+        if (gridReduce<256, 2>(v, rb, t)) applyEpi(epi, S, t[0], t[1]);
+    }
+}
+
+// The same up-leg for the 2x coarsening, one thread per coarse cell column: a
+// thread marches PZC coarse layers up z and writes the up-to-8 fine nodes
+// (2cx+{0,1}, 2cy+{0,1}, 2cz+{0,1}) of each cell.  The coarse corners are read
+// once per layer (the top corners become the next layer's bottom ones) and the
+// trilinear weights are applied separably (z, then y, then x), so the kernel
+// issues ~1.5 coarse loads per fine node instead of ~10.
+constexpr int PZC = 4;
+template <typename T>
+__global__ void __launch_bounds__(256)
+    kProlongSmooth2(Grid gf, Grid gc, const T* __restrict__ zc, const T* __restrict__ rf, const T* __restrict__ dinv,
+                    const uint8_t* __restrict__ flags, T* __restrict__ zf, double coef, int maskFixed,
+                    const T* __restrict__ aux, int epi, Scalars* S, RedBuf rb, int checkDone) {
+    if (checkDone && S->done) return;
+    const int cx = blockIdx.x * 32 + threadIdx.x, cy = blockIdx.y * 8 + threadIdx.y;
+    // even fine x / y of the cell exist (the last coarse column has no fine node
+    // when the fine element count is odd), and the odd ones
+    const bool valid = cx < gc.nx && cy < gc.ny && 2 * cx < gf.nx && 2 * cy < gf.ny;
+    const bool hx = valid && cx + 1 < gc.nx && 2 * cx + 1 < gf.nx;
+    const bool hy = valid && cy + 1 < gc.ny && 2 * cy + 1 < gf.ny;
+    const T half = T(0.5), cf = (T)coef;
+    DotAcc<T> d0, d1;
+    // Corner values of a coarse layer: [iy][ix][c], 0 where the corner does not exist.
+    auto loadLayer = [&](int cz, T (&v)[2][2][3]) {
+#pragma unroll
+        for (int iy = 0; iy < 2; ++iy)
+#pragma unroll
+            for (int ix = 0; ix < 2; ++ix) {
+                const bool ok = valid && cz < gc.nz && (ix == 0 || hx) && (iy == 0 || hy);
+                v[iy][ix][0] = v[iy][ix][1] = v[iy][ix][2] = T(0);
+                if (ok) {
+                    const T* p = zc + 3 * gc.store(cx + ix, cy + iy, cz);
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) v[iy][ix][c] = p[c];
+                }
+            }
+    };
+    // Fine layer fz from the plane values P at the cell's coarse corners.
+    auto emit = [&](int fz, const T (&P)[2][2][3]) {
+#pragma unroll
+        for (int jy = 0; jy < 2; ++jy) {
+            if (jy && !hy) continue;
+#pragma unroll
+            for (int jx = 0; jx < 2; ++jx) {
+                if (jx && !hx) continue;
+                const int64_t s = gf.store(2 * cx + jx, 2 * cy + jy, fz);
+                const uint8_t fl = flags[s];
+                T out[3] = {T(0), T(0), T(0)}, r[3] = {T(0), T(0), T(0)};
+                if (fl & FLAG_USED) {
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        const T a0 = jx ? half * (P[0][0][c] + P[0][1][c]) : P[0][0][c];
+                        const T a1 = jx ? half * (P[1][0][c] + P[1][1][c]) : P[1][0][c];
+                        const T pv = jy ? half * (a0 + a1) : a0;
+                        r[c] = rf[3 * s + c];
+                        out[c] = pv + cf * dinv[3 * s + c] * r[c];
+                    }
+                    if (maskFixed && (fl & FLAG_FIXED)) out[0] = out[1] = out[2] = T(0);
+                }
+#pragma unroll
+                for (int c = 0; c < 3; ++c) zf[3 * s + c] = out[c];
+                if (epi != EPI_NONE) {
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        d0.add(r[c] * out[c]);
+                        if (aux) d1.add(out[c] * aux[3 * s + c]);
+                    }
+                }
+            }
+        }
+    };
+    if (valid) {
+        const int cz0 = blockIdx.z * PZC, cz1 = min(gc.nz, cz0 + PZC);
+        T B[2][2][3], Tp[2][2][3], M[2][2][3];
+        loadLayer(cz0, B);
+        for (int cz = cz0; cz < cz1; ++cz) {
+            if (2 * cz >= gf.nz) break;
+            const bool hz = cz + 1 < gc.nz && 2 * cz + 1 < gf.nz;
+            emit(2 * cz, B);
+            if (hz) {
+                loadLayer(cz + 1, Tp);
+#pragma unroll
+                for (int iy = 0; iy < 2; ++iy)
+#pragma unroll
+                    for (int ix = 0; ix < 2; ++ix)
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) {
+                            M[iy][ix][c] = half * (B[iy][ix][c] + Tp[iy][ix][c]);
+                            B[iy][ix][c] = Tp[iy][ix][c];
+                        }
+                emit(2 * cz + 1, M);
             }
         }
     }
@@ -822,11 +1283,15 @@ inline dim3 nodeGrid(const Grid& g) {
 
 cudaError_t setKernelAttributes() {
     const int s64 = (kSuElems + kSyElems) * (int)sizeof(double), s32 = (kSuElems + kSyElems) * (int)sizeof(float);
+    const int sdf = (kSuElems + kSyElems) * (int)sizeof(df);
+    const cudaFuncAttribute A = cudaFuncAttributeMaxDynamicSharedMemorySize;
     cudaError_t e;
-    if ((e = cudaFuncSetAttribute(kMatvec<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, s64))) return e;
-    if ((e = cudaFuncSetAttribute(kMatvec<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, s64))) return e;
-    if ((e = cudaFuncSetAttribute(kMatvec<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, s32))) return e;
-    return cudaFuncSetAttribute(kMatvec<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, s32);
+    if ((e = cudaFuncSetAttribute(kMatvecH<double, double>, A, s64))) return e;
+    if ((e = cudaFuncSetAttribute(kMatvecH<float, float>, A, s32))) return e;
+    if ((e = cudaFuncSetAttribute(kMatvecH<double, df>, A, sdf))) return e;
+    if ((e = cudaFuncSetAttribute(kMatvec<double, false>, A, s64))) return e;
+    if ((e = cudaFuncSetAttribute(kMatvec<float, false>, A, s32))) return e;
+    return cudaFuncSetAttribute(kMatvec<double, false, df>, A, sdf);
 }
 
 template <typename T>
@@ -839,7 +1304,7 @@ int launchMatvec(const LaunchCtx& c, const MatvecArgs<T>& a, bool structured, co
         Ks<T> k;
         const T* src = static_cast<const T*>(opconst);
         for (int i = 0; i < 45; ++i) k.v[i] = src[i];
-        kMatvec<T, true><<<grid, block, smem, c.stream>>>(a, k, c.S, c.rb);
+        kMatvecH<T, T><<<grid, block, smem, c.stream>>>(a, k, c.S, c.rb);
     } else {
         Kd<T> k;
         const T* src = static_cast<const T*>(opconst) + 45;
@@ -849,11 +1314,32 @@ int launchMatvec(const LaunchCtx& c, const MatvecArgs<T>& a, bool structured, co
     return 1;
 }
 
+int launchMatvecDF(const LaunchCtx& c, const MatvecArgs<double>& a, bool structured, const double* opconst) {
+    const Grid& g = a.g;
+    dim3 grid((g.nx + MV_TX - 2) / (MV_TX - 1), (g.ny + MV_TY - 2) / (MV_TY - 1), (g.nz + MV_ZC - 1) / MV_ZC);
+    dim3 block(MV_TX, MV_TY);
+    size_t smem = (size_t)(kSuElems + kSyElems) * sizeof(df);
+    if (structured) {
+        Ks<df> k;
+        for (int i = 0; i < 45; ++i) k.v[i] = df(opconst[i]);
+        kMatvecH<double, df><<<grid, block, smem, c.stream>>>(a, k, c.S, c.rb);
+    } else {
+        Kd<df> k;
+        for (int i = 0; i < 576; ++i) k.v[i] = df(opconst[45 + i]);
+        kMatvec<double, false, df><<<grid, block, smem, c.stream>>>(a, k, c.S, c.rb);
+    }
+    return 1;
+}
+
 template <typename T>
 int launchRestrict(const LaunchCtx& c, const Grid& gf, const Grid& gc, int div, const T* rf, T* rc, int checkDone) {
-    dim3 grid = nodeGrid(gc), block(32, 8);
-    if (div == 4) kRestrict<T, 4><<<grid, block, 0, c.stream>>>(gf, gc, rf, rc, c.S, checkDone);
-    else kRestrict<T, 2><<<grid, block, 0, c.stream>>>(gf, gc, rf, rc, c.S, checkDone);
+    dim3 block(32, 8);
+    if (div == 4) {
+        kRestrict<T, 4><<<nodeGrid(gc), block, 0, c.stream>>>(gf, gc, rf, rc, c.S, checkDone);
+    } else {
+        dim3 grid((gc.nx + 31) / 32, (gc.ny + 7) / 8, (gc.nz + PZR - 1) / PZR);
+        kRestrict2<T><<<grid, block, 0, c.stream>>>(gf, gc, rf, rc, c.S, checkDone);
+    }
     return 1;
 }
 
@@ -862,7 +1348,11 @@ int launchProlongSmooth(const LaunchCtx& c, const Grid& gf, const Grid& gc, int 
                         const T* dinv, const uint8_t* flags, T* zf, double coef, int maskFixed, const T* aux, int epi,
                         int checkDone) {
     dim3 grid = nodeGrid(gf), block(32, 8);
-    if (div == 4)
+    if (div == 2) {
+        dim3 cgrid((gc.nx + 31) / 32, (gc.ny + 7) / 8, (gc.nz + PZC - 1) / PZC);
+        kProlongSmooth2<T><<<cgrid, block, 0, c.stream>>>(gf, gc, zc, rf, dinv, flags, zf, coef, maskFixed, aux, epi,
+                                                          c.S, c.rb, checkDone);
+    } else if (div == 4)
         kProlongSmooth<T, 4><<<grid, block, 0, c.stream>>>(gf, gc, zc, rf, dinv, flags, zf, coef, maskFixed, aux, epi,
                                                              c.S, c.rb, checkDone);
     else
@@ -1029,7 +1519,7 @@ cudaError_t launchMatvecNoAlloc(cudaStream_t s, const MatvecArgs<double>& a, boo
     if (structured) {
         Ks<double> k;
         for (int i = 0; i < 45; ++i) k.v[i] = static_cast<const double*>(opconst)[i];
-        kMatvec<double, true><<<grid, block, smem, s>>>(b, k, S, rb);
+        kMatvecH<double, double><<<grid, block, smem, s>>>(b, k, S, rb);
     } else {
         Kd<double> k;
         for (int i = 0; i < 576; ++i) k.v[i] = static_cast<const double*>(opconst)[45 + i];

@@ -94,6 +94,10 @@ cudaError_t setKernelAttributes();
 template <typename T>
 int launchMatvec(const LaunchCtx& c, const MatvecArgs<T>& a, bool structured, const void* opconst);
 
+// The same product on FP64 vectors in double-float arithmetic (FP32 instructions,
+// ~48-bit significands): the mixed-precision true residual.  a.y may be null.
+int launchMatvecDF(const LaunchCtx& c, const MatvecArgs<double>& a, bool structured, const double* opconst);
+
 template <typename T>
 int launchRestrict(const LaunchCtx& c, const Grid& gf, const Grid& gc, int div, const T* rf, T* rc,
                    int checkDone);

@@ -29,7 +29,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/vfem_net.h"
+#include "vfem_net.h"
 
 namespace {
 

@@ -16,7 +16,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/vfem.h"
+#include "vfem.h"
 
 namespace vfem {
 
