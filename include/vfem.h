@@ -60,9 +60,10 @@ typedef enum vfem_mg_mode {
 
 typedef enum vfem_precision {
     VFEM_PREC_FP64 = 0,     /* plain FP64 MG-PCG */
-    VFEM_PREC_MIXED = 1     /* FP32 CG + FP32 V-cycle, FP64 dots, FP64 solution accumulation,
-                               FP64 residual replacement every `replace_every` iterations and
-                               FP64 final residual check */
+    VFEM_PREC_MIXED = 1     /* FP32 CG + FP32 V-cycle, FP64 reductions, FP64 solution accumulation,
+                               true residual f - K x in double-float arithmetic substituted for the
+                               recursive one (reliable updates, `replace_delta`, `replace_every`)
+                               and checked at exit */
 } vfem_precision;
 
 typedef struct vfem_options {
@@ -73,13 +74,16 @@ typedef struct vfem_options {
     double omega;            /* damped-Jacobi weight for VFEM_MG_VCYCLE; default 0.6 */
     int32_t pre_sweeps;      /* VFEM_MG_VCYCLE only; default 1 */
     int32_t post_sweeps;     /* VFEM_MG_VCYCLE only; default 1 */
-    int32_t replace_every;   /* mixed precision: FP64 true-residual replacement period; default 50 */
+    int32_t replace_every;   /* mixed precision: also replace the residual every this many iterations;
+                                default 0 = off (replacements follow replace_delta) */
     int32_t flexible;        /* 1: flexible CG (Polak-Ribiere beta); default 0 (Fletcher-Reeves, as Eigen) */
     int32_t check_every;     /* iterations per device-side chunk between host polls; default 8 */
     int32_t compute_true_residual; /* 1: report the true FP64 residual at exit (one extra FP64 product
                                       outside the timed solve for VFEM_PREC_FP64); default 1 */
-    double replace_delta;    /* mixed precision: also replace the residual once |r| has dropped by this
-                                factor since the last replacement (reliable updates); default 0.1, 0 = off */
+    double replace_delta;    /* mixed precision: replace the residual once |r| has dropped by this
+                                factor since the last replacement (reliable updates); default 0.05,
+                                0 = off.  A recursive residual that claims convergence is always
+                                replaced and re-checked. */
     int32_t reserved[6];
 } vfem_options;
 

@@ -36,7 +36,13 @@ def test_host_helpers_without_gpu():
     ke = api.hex8_stiffness(1.0, 0.3)
     assert np.abs(ke - domains.hex8_stiffness(1.0, 0.3)).max() < 1e-15
     o = api.make_options()
-    assert o.rtol == 1e-6 and o.omega == 0.6 and o.replace_every == 50 and o.check_every == 8
+    assert o.rtol == 1e-6 and o.omega == 0.6 and o.replace_every == 0 and o.check_every == 8
+    assert o.replace_delta == 0.05
+    oc = api.Options()
+    lib.vfem_options_default(ctypes.byref(oc))  # the C defaults are the Python ones
+    for name, _ in api.Options._fields_:
+        if name != "reserved":
+            assert getattr(oc, name) == getattr(o, name) or name == "precision", name
     assert lib.vfem_status_string(0) == b"ok"
     assert lib.vfem_status_string(4) == b"not converged"
     bad = np.zeros(576)

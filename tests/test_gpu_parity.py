@@ -115,6 +115,9 @@ def test_mixed_precision_solve(case):
     # warm start from the answer: the double-float initial residual is already converged
     u2, st2 = A.solve(f, u0=u, precision="mixed")
     assert st2["iterations"] <= 1 and st2["rel_residual"] < 1e-6
+    # the polling chunk only changes how often the host looks: bit-identical answer and count
+    u3, st3 = A.solve(f, precision="mixed", check_every=3)
+    assert st3["iterations"] == st["iterations"] and np.array_equal(u3, u)
 
 
 def test_vcycle_mode_solve(case):

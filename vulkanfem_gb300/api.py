@@ -161,8 +161,8 @@ def hex8_stiffness(E=1.0, nu=0.3):
 
 
 def make_options(rtol=1e-6, max_iter=0, mg_mode="reference", precision="fp64", omega=0.6, pre_sweeps=1,
-                 post_sweeps=1, replace_every=50, flexible=False, check_every=8, compute_true_residual=True,
-                 replace_delta=0.1):
+                 post_sweeps=1, replace_every=0, flexible=False, check_every=8, compute_true_residual=True,
+                 replace_delta=0.05):
     lib = load_library()
     o = Options()
     lib.vfem_options_default(ctypes.byref(o))

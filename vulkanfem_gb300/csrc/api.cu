@@ -604,6 +604,7 @@ vfem_status solveImpl(vfem_problem* p, const vfem_options* optIn, bool haveX0, v
     }
     CK(cudaGetLastError());
     // ---- chunked iterations replayed from a cached graph
+    const int chunk = o.check_every;
     GraphKey key{o.mg_mode, o.precision, o.flexible, o.pre_sweeps, o.post_sweeps, mixed ? o.replace_every : 0,
                  o.check_every, o.omega};
     CachedGraph& cg = p->graphs[key];
@@ -611,7 +612,7 @@ vfem_status solveImpl(vfem_problem* p, const vfem_options* optIn, bool haveX0, v
         cudaGraph_t graph = nullptr;
         CK(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
         long long k = 0;
-        for (int i = 0; i < o.check_every; ++i) k += iteration(p, o, &z64, &z32);
+        for (int i = 0; i < chunk; ++i) k += iteration(p, o, &z64, &z32);
         cudaError_t ec = cudaStreamEndCapture(p->stream, &graph);
         if (ec != cudaSuccess) return fail(VFEM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ec));
         ec = cudaGraphInstantiate(&cg.exec, graph, 0);
@@ -623,7 +624,7 @@ vfem_status solveImpl(vfem_problem* p, const vfem_options* optIn, bool haveX0, v
         cg.kernels = k;
     }
     long long chunks = 0;
-    const long long maxChunks = maxIter / o.check_every + 2;
+    const long long maxChunks = maxIter / chunk + 2;
     for (;;) {
         CK(cudaMemcpyAsync(p->hS, p->S, sizeof(Scalars), cudaMemcpyDeviceToHost, p->stream));
         CK(cudaStreamSynchronize(p->stream));
@@ -714,11 +715,11 @@ void vfem_options_default(vfem_options* o) {
     o->omega = 0.6;
     o->pre_sweeps = 1;
     o->post_sweeps = 1;
-    o->replace_every = 50;
+    o->replace_every = 0;
     o->flexible = 0;
     o->check_every = 8;
     o->compute_true_residual = 1;
-    o->replace_delta = 0.1;
+    o->replace_delta = 0.05;
 }
 
 const char* vfem_status_string(vfem_status s) {

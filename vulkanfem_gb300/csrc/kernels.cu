@@ -606,7 +606,11 @@ __device__ __forceinline__ void fwht4x3(T (&v)[12]) {
 // the 256^3 workload: FP32 3 blocks per SM (80 registers, no spills; 4 blocks
 // spill and run 33% slower); FP64 and df 2 blocks per SM (128 registers, a few
 // spilled values; 20% faster than 1 block without spills).
-template <typename T, typename TC>
+//
+// CGP = true is the FP32 CG product itself (mode MV_AX, dot x.(Kx), no FP32
+// copy, no second dot) with that output stage compiled in; its per-thread dot
+// sums at most 48 terms and accumulates them with plain FMAs.
+template <typename T, typename TC, bool CGP = false>
 __global__ void __launch_bounds__(MV_TX* MV_TY, sizeof(TC) == 4 ? 3 : 2)
     kMatvecH(MatvecArgs<T> a, const Ks<TC> kp, Scalars* S, RedBuf rb) {
     if (a.checkDone && S->done) return;
@@ -672,6 +676,7 @@ __global__ void __launch_bounds__(MV_TX* MV_TY, sizeof(TC) == 4 ? 3 : 2)
 #pragma unroll
     for (int i = 0; i < 12; ++i) carry[i] = TC(0);
     DotAcc<TC> d0, d1;
+    TC dAx = TC(0);  // CGP: x.(Kx) of this thread
     gload(z0 - 1);
     sstore(z0 - 1);
     gload(z0);
@@ -740,11 +745,23 @@ __global__ void __launch_bounds__(MV_TX* MV_TY, sizeof(TC) == 4 ? 3 : 2)
             ldSlot<TC>(SY(0, ty + 1, tx + 1), q[0], q[1], q[2]);
 #pragma unroll
             for (int c = 0; c < 3; ++c) sum[c] += q[c];
-            mvOutput<T, TC>(a, (int64_t)oCol + (int64_t)k * plane, sum, (fl & FLAG_FIXED) != 0, xo, d0, d1);
+            const int64_t s = (int64_t)oCol + (int64_t)k * plane;
+            if constexpr (CGP) {
+                const bool fixed = (fl & FLAG_FIXED) != 0;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const TC out = fixed ? TC(0) : sum[c];
+                    a.y[3 * s + c] = C::out(out);
+                    dAx = fma(xo[c], out, dAx);
+                }
+            } else {
+                mvOutput<T, TC>(a, s, sum, (fl & FLAG_FIXED) != 0, xo, d0, d1);
+            }
         }
     }
 #undef SU
 #undef SY
+    if constexpr (CGP) d0.add(dAx);
     if (a.epi != EPI_NONE) {
         double v[2] = {d0.get(), d1.get()}, t[2];
         if (gridReduce<MV_TX * MV_TY, 2>(v, rb, t)) applyEpi(a.epi, S, t[0], t[1]);
@@ -1288,6 +1305,7 @@ cudaError_t setKernelAttributes() {
     cudaError_t e;
     if ((e = cudaFuncSetAttribute(kMatvecH<double, double>, A, s64))) return e;
     if ((e = cudaFuncSetAttribute(kMatvecH<float, float>, A, s32))) return e;
+    if ((e = cudaFuncSetAttribute(kMatvecH<float, float, true>, A, s32))) return e;
     if ((e = cudaFuncSetAttribute(kMatvecH<double, df>, A, sdf))) return e;
     if ((e = cudaFuncSetAttribute(kMatvec<double, false>, A, s64))) return e;
     if ((e = cudaFuncSetAttribute(kMatvec<float, false>, A, s32))) return e;
@@ -1304,6 +1322,13 @@ int launchMatvec(const LaunchCtx& c, const MatvecArgs<T>& a, bool structured, co
         Ks<T> k;
         const T* src = static_cast<const T*>(opconst);
         for (int i = 0; i < 45; ++i) k.v[i] = src[i];
+        const bool axdot = a.mode == MV_AX && a.dot0 == DOT_X_OUT && !a.dot1 && !a.y32;
+        if constexpr (std::is_same<T, float>::value) {
+            if (axdot) {
+                kMatvecH<T, T, true><<<grid, block, smem, c.stream>>>(a, k, c.S, c.rb);
+                return 1;
+            }
+        }
         kMatvecH<T, T><<<grid, block, smem, c.stream>>>(a, k, c.S, c.rb);
     } else {
         Kd<T> k;
