@@ -163,8 +163,8 @@ def algorithmic_bytes(kind, g0, g1, s):
     """Algorithmic bytes per launch on the finest level.  N = grid nodes, Ne = voxels
     (dense-grid model): matvec 6sN + Ne/8 + 4Ne + N/8 (x in, y out, occupancy bits,
     modulus, fixed bits); restrict 3sN_f + 3sN_c; prolong+smooth 3sN_c + 9sN_f (z_c,
-    r, D^-1 in; z out) + N_f/8; x/r update 18sN (FP64) or (6*8 + 12*4)N (mixed);
-    p update 9sN."""
+    r, D^-1 in; z out) + N_f/8; x/r update 18sN (x, r, p, Ap in; x, r out; the
+    mixed solve keeps its x correction in FP32 too); p update 9sN."""
     N, Ne = g0["nodes"], g0["voxels"]
     Nc = g1["nodes"]
     if kind == "matvec":
@@ -174,7 +174,7 @@ def algorithmic_bytes(kind, g0, g1, s):
     if kind == "prolong":
         return 3 * s * Nc + 9 * s * N + N / 8
     if kind == "update_xr":
-        return 18 * s * N if s == 8 else (6 * 8 + 12 * 4) * N
+        return 18 * s * N
     if kind == "update_p":
         return 9 * s * N
     raise KeyError(kind)

@@ -607,10 +607,15 @@ __device__ __forceinline__ void fwht4x3(T (&v)[12]) {
 // spill and run 33% slower); FP64 and df 2 blocks per SM (128 registers, a few
 // spilled values; 20% faster than 1 block without spills).
 //
-// CGP = true is the FP32 CG product itself (mode MV_AX, dot x.(Kx), no FP32
-// copy, no second dot) with that output stage compiled in; its per-thread dot
-// sums at most 48 terms and accumulates them with plain FMAs.
-template <typename T, typename TC, bool CGP = false>
+// OUT selects the output stage at compile time (runtime mode switches in the
+// owner stage cost ~20% of this issue-bound kernel):
+//   OUT_ANY   mvOutput with the runtime mode and dots;
+//   OUT_CG    the CG product: y = Kx (fixed rows 0), dot x.(Kx); the per-thread
+//             dot sums at most 48 terms and accumulates with plain FMAs;
+//   OUT_TRUE  the true residual: r = f - Kx, its FP32 rounding to y32, y (FP64)
+//             only when given, dot r.r.
+enum MvOut : int { OUT_ANY = 0, OUT_CG = 1, OUT_TRUE = 2 };
+template <typename T, typename TC, int OUT = OUT_ANY>
 __global__ void __launch_bounds__(MV_TX* MV_TY, sizeof(TC) == 4 ? 3 : 2)
     kMatvecH(MatvecArgs<T> a, const Ks<TC> kp, Scalars* S, RedBuf rb) {
     if (a.checkDone && S->done) return;
@@ -676,7 +681,7 @@ __global__ void __launch_bounds__(MV_TX* MV_TY, sizeof(TC) == 4 ? 3 : 2)
 #pragma unroll
     for (int i = 0; i < 12; ++i) carry[i] = TC(0);
     DotAcc<TC> d0, d1;
-    TC dAx = TC(0);  // CGP: x.(Kx) of this thread
+    TC dAx = TC(0);  // OUT_CG: x.(Kx) of this thread
     gload(z0 - 1);
     sstore(z0 - 1);
     gload(z0);
@@ -746,13 +751,22 @@ __global__ void __launch_bounds__(MV_TX* MV_TY, sizeof(TC) == 4 ? 3 : 2)
 #pragma unroll
             for (int c = 0; c < 3; ++c) sum[c] += q[c];
             const int64_t s = (int64_t)oCol + (int64_t)k * plane;
-            if constexpr (CGP) {
+            if constexpr (OUT == OUT_CG) {
                 const bool fixed = (fl & FLAG_FIXED) != 0;
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
                     const TC out = fixed ? TC(0) : sum[c];
                     a.y[3 * s + c] = C::out(out);
                     dAx = fma(xo[c], out, dAx);
+                }
+            } else if constexpr (OUT == OUT_TRUE) {
+                const bool fixed = (fl & FLAG_FIXED) != 0;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const TC out = C::in(a.f[3 * s + c]) - (fixed ? TC(0) : sum[c]);
+                    if (a.y) a.y[3 * s + c] = C::out(out);
+                    a.y32[3 * s + c] = toF(out);
+                    d0.add(out * out);
                 }
             } else {
                 mvOutput<T, TC>(a, s, sum, (fl & FLAG_FIXED) != 0, xo, d0, d1);
@@ -761,7 +775,7 @@ __global__ void __launch_bounds__(MV_TX* MV_TY, sizeof(TC) == 4 ? 3 : 2)
     }
 #undef SU
 #undef SY
-    if constexpr (CGP) d0.add(dAx);
+    if constexpr (OUT == OUT_CG) d0.add(dAx);
     if (a.epi != EPI_NONE) {
         double v[2] = {d0.get(), d1.get()}, t[2];
         if (gridReduce<MV_TX * MV_TY, 2>(v, rb, t)) applyEpi(a.epi, S, t[0], t[1]);
@@ -1305,7 +1319,9 @@ cudaError_t setKernelAttributes() {
     cudaError_t e;
     if ((e = cudaFuncSetAttribute(kMatvecH<double, double>, A, s64))) return e;
     if ((e = cudaFuncSetAttribute(kMatvecH<float, float>, A, s32))) return e;
-    if ((e = cudaFuncSetAttribute(kMatvecH<float, float, true>, A, s32))) return e;
+    if ((e = cudaFuncSetAttribute(kMatvecH<float, float, OUT_CG>, A, s32))) return e;
+    if ((e = cudaFuncSetAttribute(kMatvecH<double, double, OUT_CG>, A, s64))) return e;
+    if ((e = cudaFuncSetAttribute(kMatvecH<double, df, OUT_TRUE>, A, sdf))) return e;
     if ((e = cudaFuncSetAttribute(kMatvecH<double, df>, A, sdf))) return e;
     if ((e = cudaFuncSetAttribute(kMatvec<double, false>, A, s64))) return e;
     if ((e = cudaFuncSetAttribute(kMatvec<float, false>, A, s32))) return e;
@@ -1322,14 +1338,10 @@ int launchMatvec(const LaunchCtx& c, const MatvecArgs<T>& a, bool structured, co
         Ks<T> k;
         const T* src = static_cast<const T*>(opconst);
         for (int i = 0; i < 45; ++i) k.v[i] = src[i];
-        const bool axdot = a.mode == MV_AX && a.dot0 == DOT_X_OUT && !a.dot1 && !a.y32;
-        if constexpr (std::is_same<T, float>::value) {
-            if (axdot) {
-                kMatvecH<T, T, true><<<grid, block, smem, c.stream>>>(a, k, c.S, c.rb);
-                return 1;
-            }
-        }
-        kMatvecH<T, T><<<grid, block, smem, c.stream>>>(a, k, c.S, c.rb);
+        if (a.mode == MV_AX && a.dot0 == DOT_X_OUT && !a.dot1 && !a.y32)
+            kMatvecH<T, T, OUT_CG><<<grid, block, smem, c.stream>>>(a, k, c.S, c.rb);
+        else
+            kMatvecH<T, T><<<grid, block, smem, c.stream>>>(a, k, c.S, c.rb);
     } else {
         Kd<T> k;
         const T* src = static_cast<const T*>(opconst) + 45;
@@ -1347,7 +1359,10 @@ int launchMatvecDF(const LaunchCtx& c, const MatvecArgs<double>& a, bool structu
     if (structured) {
         Ks<df> k;
         for (int i = 0; i < 45; ++i) k.v[i] = df(opconst[i]);
-        kMatvecH<double, df><<<grid, block, smem, c.stream>>>(a, k, c.S, c.rb);
+        if (a.mode == MV_RESID && a.dot0 == DOT_OUT_OUT && !a.dot1 && a.y32)
+            kMatvecH<double, df, OUT_TRUE><<<grid, block, smem, c.stream>>>(a, k, c.S, c.rb);
+        else
+            kMatvecH<double, df><<<grid, block, smem, c.stream>>>(a, k, c.S, c.rb);
     } else {
         Kd<df> k;
         for (int i = 0; i < 576; ++i) k.v[i] = df(opconst[45 + i]);
