@@ -215,3 +215,34 @@ def test_per_voxel_modulus():
     assert rel(A3 @ x, y_ref) < 1e-12
     u3, st3 = A3.solve(f, mg_mode="vcycle")
     assert st3["rel_residual"] < 1e-6
+
+
+def test_setup_rejects_bad_input_with_status_codes():
+    """The device set-up reports invalid input as status codes and leaves the
+    library usable (VFEM_ERR_INVALID_ARGUMENT = 1, VFEM_ERR_EMPTY = 7)."""
+    import ctypes
+    lib = api.load_library()
+    ke = np.ascontiguousarray(domains.hex8_stiffness().reshape(-1))
+    vox = np.ones((4, 5, 6), np.uint8)
+    fixed = np.arange(7 * 6, dtype=np.int64)  # the z = 0 face of the full box
+
+    def create(v, E=None, fx=fixed):
+        h = ctypes.c_void_p()
+        Ep = None if E is None else np.ascontiguousarray(E, np.float32).ctypes.data_as(ctypes.c_void_p)
+        s = lib.vfem_problem_create(np.ascontiguousarray(v).reshape(-1), v.shape[2], v.shape[1], v.shape[0], ke,
+                                    Ep, fx, fx.size, 2, 0, ctypes.byref(h))
+        if h.value:
+            lib.vfem_problem_destroy(h)
+        return s
+
+    bad = vox.copy()
+    bad[1, 2, 3] = 2
+    assert create(bad) == 1
+    E = np.ones(vox.shape, np.float32)
+    E[0, 0, 0] = 0.0
+    assert create(vox, E) == 1
+    E[0, 0, 0] = np.nan
+    assert create(vox, E) == 1
+    assert create(np.zeros_like(vox)) == 7
+    assert create(vox, fx=np.array([10 ** 6], np.int64)) == 1
+    assert create(vox) == 0

@@ -20,9 +20,11 @@
 #include <map>
 #include <string>
 #include <tuple>
+#include <type_traits>
 #include <vector>
 
 #include "kernels.h"
+#include "setup_gpu.h"
 
 using namespace vfem;
 
@@ -71,8 +73,10 @@ struct vfem_problem {
     int device = 0;
     cudaStream_t stream = nullptr;
     KeData ke;
-    Hierarchy H;
     std::vector<DevLevel> L;
+    // coarsest level (built from its device flags at set-up)
+    std::vector<int32_t> coarseFreeDof;   // storage DOF index (3*s + c) of each free coarse DOF
+    std::vector<int32_t> coarseFreeNode;  // storage node -> free node id, -1 otherwise
     // level-0 solver vectors (dense storage)
     double *f64 = nullptr, *x64 = nullptr, *p64 = nullptr, *Ap64 = nullptr;
     float *p32 = nullptr, *Ap32 = nullptr;
@@ -80,10 +84,14 @@ struct vfem_problem {
     // coarsest dense inverse
     int64_t nc = 0;
     int32_t* freeDof = nullptr;
+    // Coarsest dense inverses, built on first use (ensureCoarse): FP64 for the
+    // FP64 solver and preconditioner, FP32 for the mixed one; V = the
+    // multiplicative cycle's operator (volume-averaged modulus).
     double* Kinv64 = nullptr;
     float* Kinv32 = nullptr;
-    double* KinvV64 = nullptr;  // multiplicative cycle's coarsest inverse (volume-averaged modulus)
+    double* KinvV64 = nullptr;
     float* KinvV32 = nullptr;
+    int32_t* dFreeNode = nullptr;  // coarsest storage node -> free node id (assembly)
     double* cb64 = nullptr;
     float* cb32 = nullptr;
     // reductions / scalars
@@ -146,7 +154,7 @@ void freeProblem(vfem_problem* p) {
     cudaFree(p->f64); cudaFree(p->x64); cudaFree(p->p64); cudaFree(p->Ap64); cudaFree(p->p32); cudaFree(p->Ap32);
     cudaFree(p->x32);
     cudaFree(p->freeDof); cudaFree(p->Kinv64); cudaFree(p->Kinv32); cudaFree(p->cb64); cudaFree(p->cb32);
-    cudaFree(p->KinvV64); cudaFree(p->KinvV32);
+    cudaFree(p->KinvV64); cudaFree(p->KinvV32); cudaFree(p->dFreeNode);
     cudaFree(p->S); cudaFree(p->rb.partials); cudaFree(p->rb.ticket); cudaFree(p->dComp);
     if (p->hS) cudaFreeHost(p->hS);
     if (p->hIn) cudaFreeHost(p->hIn);
@@ -157,65 +165,111 @@ void freeProblem(vfem_problem* p) {
 
 LaunchCtx ctx(vfem_problem* p) { return LaunchCtx{p->stream, p->S, p->rb}; }
 
-vfem_status invertCoarse(vfem_problem* p, const int32_t* dFreeNode, const float* E, double scale, double* K64,
-                         float* K32);
+template <typename T>
+vfem_status invertCoarse(vfem_problem* p, const float* E, double scale, T* K);
 
 vfem_status buildCoarse(vfem_problem* p) {
-    const HostLevel& hc = p->H.L.back();
     DevLevel& dc = p->L.back();
-    int64_t n = (int64_t)p->H.coarseFreeDof.size();
+    // Coarsest free DOFs (FEM.cpp:473-496), in compressed (storage) order, from the level's flags.
+    {
+        std::vector<uint8_t> fl((size_t)dc.g.nnode);
+        CK(cudaMemcpyAsync(fl.data(), dc.flags, fl.size(), cudaMemcpyDeviceToHost, p->stream));
+        CK(cudaStreamSynchronize(p->stream));
+        p->coarseFreeDof.clear();
+        p->coarseFreeNode.assign(fl.size(), -1);
+        int32_t nf = 0;
+        for (size_t s = 0; s < fl.size(); ++s) {
+            if (!(fl[s] & FLAG_USED) || (fl[s] & FLAG_FIXED)) continue;
+            p->coarseFreeNode[s] = nf++;
+            for (int c = 0; c < 3; ++c) p->coarseFreeDof.push_back((int32_t)(3 * s + c));
+        }
+    }
+    int64_t n = (int64_t)p->coarseFreeDof.size();
     p->nc = n;
     if (n > kMaxCoarseFree)
         return fail(VFEM_ERR_COARSE_TOO_LARGE, "coarsest level has " + std::to_string(n) +
                                                    " free DOFs; add levels (limit " +
                                                    std::to_string(kMaxCoarseFree) + ")");
     if (n == 0) return VFEM_OK;
-    CK(upload(&p->freeDof, p->H.coarseFreeDof));
-    int32_t* dFreeNode = nullptr;
-    CK(upload(&dFreeNode, p->H.coarseFreeNode));
-    CK(dalloc(&p->Kinv64, n * n));
-    CK(dalloc(&p->Kinv32, n * n));
-    CK(dalloc(&p->KinvV64, n * n));
-    CK(dalloc(&p->KinvV32, n * n));
+    CK(upload(&p->freeDof, p->coarseFreeDof));
+    CK(upload(&p->dFreeNode, p->coarseFreeNode));
     CK(dalloc(&p->cb64, n));
     CK(dalloc(&p->cb32, n));
-    // Kc = 2^(L-1+skip) sum_e E_e Ke on the free DOFs (assembleK, FEM.cpp:19-63,498-513),
-    // and the same with the volume-averaged modulus for the multiplicative cycle.
-    vfem_status st = invertCoarse(p, dFreeNode, dc.E, hc.scale, p->Kinv64, p->Kinv32);
-    if (st == VFEM_OK) st = invertCoarse(p, dFreeNode, dc.Ev, hc.scale, p->KinvV64, p->KinvV32);
-    cudaFree(dFreeNode);
-    return st;
+    return VFEM_OK;
 }
 
-// Dense Cholesky (cuSOLVER potrf) and inverse (potri) of scale * sum_e E_e Ke on
-// the coarsest free DOFs, symmetrised, with an FP32 copy.
-vfem_status invertCoarse(vfem_problem* p, const int32_t* dFreeNode, const float* E, double scale, double* K64,
-                         float* K32) {
+// cuSOLVER's dense Cholesky factorisation and inverse by scalar type.
+struct SolverFp64 {
+    typedef double T;
+    static cusolverStatus_t potrfBuf(cusolverDnHandle_t h, int n, T* A, int* lw) {
+        return cusolverDnDpotrf_bufferSize(h, CUBLAS_FILL_MODE_LOWER, n, A, n, lw);
+    }
+    static cusolverStatus_t potriBuf(cusolverDnHandle_t h, int n, T* A, int* lw) {
+        return cusolverDnDpotri_bufferSize(h, CUBLAS_FILL_MODE_LOWER, n, A, n, lw);
+    }
+    static cusolverStatus_t potrf(cusolverDnHandle_t h, int n, T* A, T* w, int lw, int* info) {
+        return cusolverDnDpotrf(h, CUBLAS_FILL_MODE_LOWER, n, A, n, w, lw, info);
+    }
+    static cusolverStatus_t potri(cusolverDnHandle_t h, int n, T* A, T* w, int lw, int* info) {
+        return cusolverDnDpotri(h, CUBLAS_FILL_MODE_LOWER, n, A, n, w, lw, info);
+    }
+};
+struct SolverFp32 {
+    typedef float T;
+    static cusolverStatus_t potrfBuf(cusolverDnHandle_t h, int n, T* A, int* lw) {
+        return cusolverDnSpotrf_bufferSize(h, CUBLAS_FILL_MODE_LOWER, n, A, n, lw);
+    }
+    static cusolverStatus_t potriBuf(cusolverDnHandle_t h, int n, T* A, int* lw) {
+        return cusolverDnSpotri_bufferSize(h, CUBLAS_FILL_MODE_LOWER, n, A, n, lw);
+    }
+    static cusolverStatus_t potrf(cusolverDnHandle_t h, int n, T* A, T* w, int lw, int* info) {
+        return cusolverDnSpotrf(h, CUBLAS_FILL_MODE_LOWER, n, A, n, w, lw, info);
+    }
+    static cusolverStatus_t potri(cusolverDnHandle_t h, int n, T* A, T* w, int lw, int* info) {
+        return cusolverDnSpotri(h, CUBLAS_FILL_MODE_LOWER, n, A, n, w, lw, info);
+    }
+};
+template <typename T>
+struct SolverOf;
+template <>
+struct SolverOf<double> {
+    typedef SolverFp64 type;
+};
+template <>
+struct SolverOf<float> {
+    typedef SolverFp32 type;
+};
+
+// K = inverse of Kc = scale * sum_e E_e Ke on the coarsest free DOFs (assembleK,
+// FEM.cpp:19-63,498-513): assembled on the GPU in T, cuSOLVER Cholesky (potrf)
+// and inverse (potri) in T, symmetrised.  The FP32 inverse is factorised in
+// FP32 (tens of milliseconds instead of seconds for the FP64 one on GB300).
+template <typename T>
+vfem_status invertCoarse(vfem_problem* p, const float* E, double scale, T* K) {
+    typedef typename SolverOf<T>::type Sv;
     DevLevel& dc = p->L.back();
     const int64_t n = p->nc;
-    p->launches += launchAssembleCoarse(p->stream, dc.g, E, dFreeNode, p->ke.Ke, scale, K64, n);
+    CK(cudaMemsetAsync(K, 0, sizeof(T) * (size_t)(n * n), p->stream));
+    p->launches += launchAssembleCoarse<T>(p->stream, dc.g, E, p->dFreeNode, p->ke.Ke, scale, K, n);
     CK(cudaGetLastError());
     cusolverDnHandle_t h = nullptr;
     if (cusolverDnCreate(&h) != CUSOLVER_STATUS_SUCCESS) return fail(VFEM_ERR_CUDA, "cusolverDnCreate failed");
     cusolverDnSetStream(h, p->stream);
     int lw1 = 0, lw2 = 0;
     vfem_status st = VFEM_OK;
-    double* work = nullptr;
+    T* work = nullptr;
     int* info = nullptr;
     int hinfo = 0;
-    if (cusolverDnDpotrf_bufferSize(h, CUBLAS_FILL_MODE_LOWER, (int)n, K64, (int)n, &lw1) !=
-            CUSOLVER_STATUS_SUCCESS ||
-        cusolverDnDpotri_bufferSize(h, CUBLAS_FILL_MODE_LOWER, (int)n, K64, (int)n, &lw2) !=
-            CUSOLVER_STATUS_SUCCESS) {
+    if (Sv::potrfBuf(h, (int)n, K, &lw1) != CUSOLVER_STATUS_SUCCESS ||
+        Sv::potriBuf(h, (int)n, K, &lw2) != CUSOLVER_STATUS_SUCCESS)
         st = fail(VFEM_ERR_CUDA, "cusolver buffer size query failed");
-    }
-    if (st == VFEM_OK && (cudaMalloc(&work, sizeof(double) * (size_t)std::max(1, std::max(lw1, lw2))) != cudaSuccess ||
+    const int lw = std::max(1, std::max(lw1, lw2));
+    if (st == VFEM_OK && (cudaMalloc(&work, sizeof(T) * (size_t)lw) != cudaSuccess ||
                           cudaMalloc(&info, sizeof(int)) != cudaSuccess))
         st = fail(VFEM_ERR_OUT_OF_MEMORY, "cusolver workspace");
     if (st == VFEM_OK) {
-        if (cusolverDnDpotrf(h, CUBLAS_FILL_MODE_LOWER, (int)n, K64, (int)n, work, std::max(lw1, lw2), info) !=
-            CUSOLVER_STATUS_SUCCESS)
-            st = fail(VFEM_ERR_CUDA, "cusolverDnDpotrf failed");
+        if (Sv::potrf(h, (int)n, K, work, lw, info) != CUSOLVER_STATUS_SUCCESS)
+            st = fail(VFEM_ERR_CUDA, "cusolver potrf failed");
         else {
             cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, p->stream);
             cudaStreamSynchronize(p->stream);
@@ -224,9 +278,8 @@ vfem_status invertCoarse(vfem_problem* p, const int32_t* dFreeNode, const float*
         }
     }
     if (st == VFEM_OK) {
-        if (cusolverDnDpotri(h, CUBLAS_FILL_MODE_LOWER, (int)n, K64, (int)n, work, std::max(lw1, lw2), info) !=
-            CUSOLVER_STATUS_SUCCESS)
-            st = fail(VFEM_ERR_CUDA, "cusolverDnDpotri failed");
+        if (Sv::potri(h, (int)n, K, work, lw, info) != CUSOLVER_STATUS_SUCCESS)
+            st = fail(VFEM_ERR_CUDA, "cusolver potri failed");
         else {
             cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, p->stream);
             cudaStreamSynchronize(p->stream);
@@ -235,14 +288,159 @@ vfem_status invertCoarse(vfem_problem* p, const int32_t* dFreeNode, const float*
         }
     }
     if (st == VFEM_OK) {
-        p->launches += launchSymmetrizeLowerToFull(p->stream, K64, n);
-        p->launches += launchConvert<double, float>(p->stream, n * n, K64, K32);
+        p->launches += launchSymmetrizeLowerToFull<T>(p->stream, K, n);
         if (cudaStreamSynchronize(p->stream) != cudaSuccess) st = fail(VFEM_ERR_CUDA, "coarse inverse kernels");
     }
     cudaFree(work);
     cudaFree(info);
     cusolverDnDestroy(h);
     return st;
+}
+
+template <typename T>
+T*& kinvSlot(vfem_problem* p, bool v);
+template <>
+double*& kinvSlot<double>(vfem_problem* p, bool v) { return v ? p->KinvV64 : p->Kinv64; }
+template <>
+float*& kinvSlot<float>(vfem_problem* p, bool v) { return v ? p->KinvV32 : p->Kinv32; }
+
+// Build the coarsest inverse a solve or preconditioner of this type and cycle
+// needs (once).  An FP32 factorisation that fails (a system too ill-conditioned
+// for FP32) falls back to the FP64 inverse rounded to FP32.
+template <typename T>
+vfem_status ensureCoarse(vfem_problem* p, bool vcycle) {
+    if (p->nc == 0) return VFEM_OK;
+    T*& K = kinvSlot<T>(p, vcycle);
+    if (K) return VFEM_OK;
+    T* buf = nullptr;
+    CK(dalloc(&buf, p->nc * p->nc));
+    const DevLevel& dc = p->L.back();
+    vfem_status st = invertCoarse<T>(p, vcycle ? dc.Ev : dc.E, dc.scale, buf);
+    if (st == VFEM_ERR_SINGULAR && std::is_same<T, float>::value) {
+        st = ensureCoarse<double>(p, vcycle);
+        if (st == VFEM_OK) {
+            launchConvert<double, T>(p->stream, p->nc * p->nc, kinvSlot<double>(p, vcycle), buf);
+            ++p->launches;
+            if (cudaStreamSynchronize(p->stream) != cudaSuccess) st = fail(VFEM_ERR_CUDA, "coarse inverse copy");
+        }
+    }
+    if (st != VFEM_OK) {
+        cudaFree(buf);
+        return st;
+    }
+    K = buf;
+    return VFEM_OK;
+}
+
+// The hierarchy on the device (setup_gpu.cu): per level the element moduli,
+// node flags, compressed numbering and inverse diagonals.  Only the level plan,
+// the Galerkin child tables, the fixed-id check and the counters touch the host.
+vfem_status buildHierarchyDevice(vfem_problem* p, const std::vector<LevelPlan>& plan, const uint8_t* vox,
+                                 const float* Ein, const int64_t* fixed, int64_t nfixed) {
+    const int L = (int)plan.size();
+    p->L.resize(L);
+    cudaStream_t st = p->stream;
+    Diag24 dg;
+    for (int i = 0; i < 24; ++i) dg.v[i] = p->ke.diag[i];
+    SetupCounters* dcnt = nullptr;
+    std::vector<SetupCounters> hcnt(L);
+    CK(dalloc(&dcnt, (int64_t)L));
+    int* scratch = nullptr;
+    uint8_t* dvox = nullptr;
+    float* dEin = nullptr;
+    double* dtab = nullptr;
+    int64_t* dfixed = nullptr;
+    vfem_status result = VFEM_OK;
+    auto cleanup = [&]() {
+        cudaFree(dcnt); cudaFree(scratch); cudaFree(dvox); cudaFree(dEin); cudaFree(dtab); cudaFree(dfixed);
+    };
+#define CKS(call)                                                                                        \
+    do {                                                                                                 \
+        cudaError_t e_ = (call);                                                                         \
+        if (e_ != cudaSuccess) {                                                                         \
+            cleanup();                                                                                   \
+            return fail(e_ == cudaErrorMemoryAllocation ? VFEM_ERR_OUT_OF_MEMORY : VFEM_ERR_CUDA,         \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                             \
+        }                                                                                                \
+    } while (0)
+    const Grid& g0 = plan[0].g;
+    const int64_t nvox = (int64_t)g0.ex * g0.ey * g0.ez;
+    CKS(dalloc(&scratch, compactScratchInts(g0.nnode)));
+    CKS(dalloc(&dvox, nvox));
+    CKS(cudaMemcpyAsync(dvox, vox, (size_t)nvox, cudaMemcpyHostToDevice, st));
+    if (Ein) {
+        CKS(dalloc(&dEin, nvox));
+        CKS(cudaMemcpyAsync(dEin, Ein, sizeof(float) * (size_t)nvox, cudaMemcpyHostToDevice, st));
+    }
+    for (int i = 0; i < L; ++i) {
+        DevLevel& d = p->L[i];
+        d.g = plan[i].g;
+        d.div = plan[i].div;
+        d.scale = plan[i].scale;
+        const int64_t nn = d.g.nnode, nv = d.nvec();
+        CKS(dalloc(&d.E, nn));
+        CKS(dalloc(&d.flags, nn));
+        CKS(dalloc(&d.dinv64, nv)); CKS(dalloc(&d.dinv32, nv));
+        CKS(dalloc(&d.dinvR64, nv)); CKS(dalloc(&d.dinvR32, nv));
+        SetupCounters* c = dcnt + i;
+        if (i == 0) {
+            d.Ev = d.E;
+            CKS(gpuLevel0(st, d.g, dvox, dEin, d.E, d.flags, c));
+        } else {
+            const DevLevel& f = p->L[i - 1];
+            CKS(dalloc(&d.Ev, nn));
+            CKS(gpuCoarseLevel(st, f.g, d.g, d.div, f.E, f.Ev, f.flags, d.E, d.Ev, d.flags, c));
+        }
+        // compressed numbering: sized by the node count, trimmed below
+        int32_t* store = nullptr;
+        CKS(dalloc(&store, nn));
+        CKS(gpuCompactUsed(st, d.g, d.flags, scratch, store, c));
+        CKS(cudaMemcpyAsync(&hcnt[i], c, sizeof(SetupCounters), cudaMemcpyDeviceToHost, st));
+        CKS(cudaStreamSynchronize(st));
+        if (i == 0) {
+            if (hcnt[0].err & 2u) result = fail(VFEM_ERR_INVALID_ARGUMENT, "voxel values must be 0 or 1");
+            else if (hcnt[0].err & 1u)
+                result = fail(VFEM_ERR_INVALID_ARGUMENT, "non-positive or non-finite modulus on a filled voxel");
+            else if (hcnt[0].filled == 0) result = fail(VFEM_ERR_EMPTY, "no filled voxel");
+            for (int64_t k = 0; result == VFEM_OK && k < nfixed; ++k)
+                if (fixed[k] < 0 || fixed[k] >= hcnt[0].nused)
+                    result = fail(VFEM_ERR_INVALID_ARGUMENT, "fixed node id out of range");
+        }
+        if (result != VFEM_OK) {
+            cudaFree(store);
+            cleanup();
+            return result;
+        }
+        d.nused = hcnt[i].nused;
+        d.nelem = (int64_t)hcnt[i].nelem;
+        CKS(dalloc(&d.nodeStore, d.nused));
+        CKS(cudaMemcpyAsync(d.nodeStore, store, sizeof(int32_t) * (size_t)d.nused, cudaMemcpyDeviceToDevice, st));
+        CKS(cudaStreamSynchronize(st));
+        cudaFree(store);
+        if (i == 0) {
+            if (nfixed > 0) {
+                CKS(dalloc(&dfixed, nfixed));
+                CKS(cudaMemcpyAsync(dfixed, fixed, sizeof(int64_t) * (size_t)nfixed, cudaMemcpyHostToDevice, st));
+                CKS(gpuSetFixed(st, nfixed, dfixed, d.nodeStore, d.flags));
+            }
+            CKS(gpuDiagRedisc(st, d.g, d.E, d.flags, d.scale, dg, d.dinv64, d.dinv32));
+        } else {
+            const DevLevel& f = p->L[i - 1];
+            std::vector<double> tab;
+            childDiagTable(p->ke.Ke, d.div, tab);
+            cudaFree(dtab);
+            dtab = nullptr;
+            CKS(upload(&dtab, tab));
+            CKS(gpuDiagCoarse(st, f.g, d.g, d.div, f.E, d.E, d.flags, d.scale, std::pow(2.0, i - 1), dtab, dg,
+                              d.dinv64, d.dinv32));
+        }
+        CKS(gpuDiagRedisc(st, d.g, d.Ev, d.flags, d.scale, dg, d.dinvR64, d.dinvR32));
+        p->launches += 8;
+    }
+    CKS(cudaStreamSynchronize(st));
+#undef CKS
+    cleanup();
+    return VFEM_OK;
 }
 
 vfem_status createImpl(const uint8_t* vox, int nx, int ny, int nz, const double* Ke, const float* E,
@@ -272,7 +470,8 @@ vfem_status createImpl(const uint8_t* vox, int nx, int ny, int nz, const double*
         }
     }
     std::string err;
-    st = buildHierarchy(vox, nx, ny, nz, E, fixed, nfixed, numLevels, skip, p->ke, p->H, err);
+    std::vector<LevelPlan> plan;
+    st = planLevels(nx, ny, nz, numLevels, skip, plan, err);
     if (st != VFEM_OK) {
         delete p;
         return fail(st, err);
@@ -298,28 +497,10 @@ vfem_status createImpl(const uint8_t* vox, int nx, int ny, int nz, const double*
     } while (0)
     CKP(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking));
     CKP(setKernelAttributes());
-    p->L.resize(p->H.L.size());
-    for (size_t i = 0; i < p->H.L.size(); ++i) {
-        const HostLevel& h = p->H.L[i];
-        DevLevel& d = p->L[i];
-        d.g = h.g;
-        d.div = h.divider;
-        d.scale = h.scale;
-        d.nused = (int64_t)h.nodeStore.size();
-        d.nelem = h.nelem;
-        CKP(upload(&d.E, h.E));
-        if (i == 0) d.Ev = d.E;
-        else CKP(upload(&d.Ev, h.Ev));
-        CKP(upload(&d.flags, h.flags));
-        CKP(upload(&d.nodeStore, h.nodeStore));
-        CKP(upload(&d.dinv64, h.dinv));
-        CKP(upload(&d.dinvR64, h.dinvRedisc));
+    st = buildHierarchyDevice(p, plan, vox, E, fixed, nfixed);
+    if (st != VFEM_OK) return bail(st);
+    for (DevLevel& d : p->L) {
         int64_t nv = d.nvec();
-        CKP(dalloc(&d.dinv32, nv));
-        CKP(dalloc(&d.dinvR32, nv));
-        launchConvert<double, float>(p->stream, nv, d.dinv64, d.dinv32);
-        launchConvert<double, float>(p->stream, nv, d.dinvR64, d.dinvR32);
-        p->launches += 2;
         CKP(dalloc(&d.r64, nv)); CKP(dalloc(&d.z64, nv)); CKP(dalloc(&d.t64, nv));
         CKP(dalloc(&d.r32, nv)); CKP(dalloc(&d.z32, nv)); CKP(dalloc(&d.t32, nv));
     }
@@ -334,6 +515,7 @@ vfem_status createImpl(const uint8_t* vox, int nx, int ny, int nz, const double*
     CKP(cudaMallocHost((void**)&p->hIn, sizeof(double) * 3 * (size_t)std::max<int64_t>(1, p->L[0].nused)));
     CKP(cudaMallocHost((void**)&p->hOut, sizeof(double) * 3 * (size_t)std::max<int64_t>(1, p->L[0].nused)));
     st = buildCoarse(p);
+    if (st == VFEM_OK) st = ensureCoarse<float>(p, false);  // the mixed solver's, and a check that Kc is SPD
     if (st != VFEM_OK) return bail(st);
     CKP(cudaStreamSynchronize(p->stream));
     CKP(cudaGetLastError());
@@ -563,6 +745,9 @@ vfem_status solveImpl(vfem_problem* p, const vfem_options* optIn, bool haveX0, v
     vfem_status s = checkOptions(o);
     if (s != VFEM_OK) return s;
     CK(cudaSetDevice(p->device));
+    s = o.precision == VFEM_PREC_FP64 ? ensureCoarse<double>(p, o.mg_mode == VFEM_MG_VCYCLE)
+                                      : ensureCoarse<float>(p, o.mg_mode == VFEM_MG_VCYCLE);
+    if (s != VFEM_OK) return s;
     DevLevel& l0 = p->L[0];
     const int64_t n = l0.nvec();
     const long long maxIter = o.max_iter > 0 ? o.max_iter : 2 * 3 * l0.nused;
@@ -854,7 +1039,9 @@ vfem_status vfem_apply_preconditioner(vfem_problem* p, int32_t mg_mode, const do
         return fail(VFEM_ERR_INVALID_ARGUMENT, "bad argument");
     CK(cudaSetDevice(p->device));
     DevLevel& l0 = p->L[0];
-    vfem_status s = toDenseHost(p, 0, r, l0.r64, nullptr);
+    vfem_status s = ensureCoarse<double>(p, mg_mode == VFEM_MG_VCYCLE);
+    if (s != VFEM_OK) return s;
+    s = toDenseHost(p, 0, r, l0.r64, nullptr);
     if (s != VFEM_OK) return s;
     vfem_options o;
     vfem_options_default(&o);
@@ -907,6 +1094,9 @@ vfem_status vfem_interpolate(vfem_problem* p, int32_t level, const double* coars
 vfem_status vfem_profile_kernels(vfem_problem* p, int32_t reps, double* ms) {
     if (!p || !ms || reps < 1) return fail(VFEM_ERR_INVALID_ARGUMENT, "bad argument");
     CK(cudaSetDevice(p->device));
+    vfem_status sc = ensureCoarse<double>(p, false);
+    if (sc == VFEM_OK) sc = ensureCoarse<float>(p, false);
+    if (sc != VFEM_OK) return sc;
     DevLevel& l0 = p->L[0];
     const bool two = p->L.size() > 1;
     DevLevel& l1 = p->L[two ? 1 : 0];
@@ -997,11 +1187,21 @@ vfem_status vfem_inverse_diagonal(vfem_problem* p, int32_t level, double* out) {
 }
 
 vfem_status vfem_fixed_nodes(vfem_problem* p, int32_t level, int64_t* out, int64_t cap, int64_t* count) {
-    if (!p || level < 0 || level >= (int)p->H.L.size()) return fail(VFEM_ERR_INVALID_ARGUMENT, "bad argument");
-    const auto& f = p->H.L[level].fixedIds;
-    if (count) *count = (int64_t)f.size();
-    if (out)
-        for (int64_t i = 0; i < std::min<int64_t>(cap, (int64_t)f.size()); ++i) out[i] = f[i];
+    if (!p || level < 0 || level >= (int)p->L.size()) return fail(VFEM_ERR_INVALID_ARGUMENT, "bad argument");
+    CK(cudaSetDevice(p->device));
+    const DevLevel& l = p->L[level];
+    std::vector<uint8_t> fl((size_t)l.g.nnode);
+    std::vector<int32_t> store((size_t)l.nused);
+    CK(cudaMemcpyAsync(fl.data(), l.flags, fl.size(), cudaMemcpyDeviceToHost, p->stream));
+    CK(cudaMemcpyAsync(store.data(), l.nodeStore, sizeof(int32_t) * store.size(), cudaMemcpyDeviceToHost, p->stream));
+    CK(cudaStreamSynchronize(p->stream));
+    int64_t n = 0;
+    for (size_t i = 0; i < store.size(); ++i) {
+        if (!(fl[store[i]] & FLAG_FIXED)) continue;
+        if (out && n < cap) out[n] = (int64_t)i;
+        ++n;
+    }
+    if (count) *count = n;
     return VFEM_OK;
 }
 

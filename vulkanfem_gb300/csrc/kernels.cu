@@ -844,39 +844,36 @@ __global__ void __launch_bounds__(256) kRestrict2(Grid gf, Grid gc, const T* __r
     const bool valid = cx < gc.nx && cy < gc.ny;
     const T half = T(0.5);
     const int fx0 = 2 * cx;
-    // Weighted row sum at fine row fy of layer fz into s[3]; all lanes take part
-    // (shuffles), out-of-grid fine nodes count 0.
-    auto rowSum = [&](int fy, int fz, T (&s)[3]) {
-        const bool rowOk = fy >= 0 && fy < gf.ny && fz >= 0 && fz < gf.nz;
-        const int64_t base = rowOk ? gf.store(0, fy, fz) : 0;
-        T c0[3] = {T(0), T(0), T(0)}, c1[3] = {T(0), T(0), T(0)}, cm[3] = {T(0), T(0), T(0)};
-        if (rowOk && fx0 < gf.nx) {
-            const T* p = rf + 3 * (base + fx0);
-            c0[0] = p[0]; c0[1] = p[1]; c0[2] = p[2];
-        }
-        if (rowOk && fx0 + 1 < gf.nx) {
-            const T* p = rf + 3 * (base + fx0 + 1);
-            c1[0] = p[0]; c1[1] = p[1]; c1[2] = p[2];
-        }
+    // Weighted plane sum at fine layer fz: the three rows 2cy-1 .. 2cy+1, each
+    // r(2cx-1)/2 + r(2cx) + r(2cx+1)/2.  All loads of the plane are issued first,
+    // then the shuffles; all lanes take part, out-of-grid fine nodes count 0.
+    auto planeSum = [&](int fz, T (&P)[3]) {
+        T c0[3][3], c1[3][3], cl[3][3];
 #pragma unroll
-        for (int c = 0; c < 3; ++c) cm[c] = __shfl_up_sync(0xffffffffu, c1[c], 1);
-        if (lane == 0) {
-            cm[0] = cm[1] = cm[2] = T(0);
-            if (rowOk && fx0 - 1 >= 0 && fx0 - 1 < gf.nx) {
-                const T* p = rf + 3 * (base + fx0 - 1);
-                cm[0] = p[0]; cm[1] = p[1]; cm[2] = p[2];
+        for (int r = 0; r < 3; ++r) {
+            const int fy = 2 * cy - 1 + r;
+            const bool rowOk = fy >= 0 && fy < gf.ny && fz >= 0 && fz < gf.nz;
+            const int64_t base = rowOk ? gf.store(0, fy, fz) : 0;
+            const bool ok0 = rowOk && fx0 < gf.nx, ok1 = rowOk && fx0 + 1 < gf.nx;
+            const bool okl = lane == 0 && rowOk && fx0 - 1 >= 0 && fx0 - 1 < gf.nx;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                c0[r][c] = ok0 ? rf[3 * (base + fx0) + c] : T(0);
+                c1[r][c] = ok1 ? rf[3 * (base + fx0 + 1) + c] : T(0);
+                cl[r][c] = okl ? rf[3 * (base + fx0 - 1) + c] : T(0);
             }
         }
+        T row[3][3];
 #pragma unroll
-        for (int c = 0; c < 3; ++c) s[c] = c0[c] + half * (cm[c] + c1[c]);
-    };
-    auto planeSum = [&](int fz, T (&P)[3]) {
-        T a[3], b[3], d[3];
-        rowSum(2 * cy - 1, fz, a);
-        rowSum(2 * cy, fz, b);
-        rowSum(2 * cy + 1, fz, d);
+        for (int r = 0; r < 3; ++r)
 #pragma unroll
-        for (int c = 0; c < 3; ++c) P[c] = b[c] + half * (a[c] + d[c]);
+            for (int c = 0; c < 3; ++c) {
+                T cm = __shfl_up_sync(0xffffffffu, c1[r][c], 1);
+                if (lane == 0) cm = cl[r][c];
+                row[r][c] = c0[r][c] + half * (cm + c1[r][c]);
+            }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) P[c] = row[1][c] + half * (row[0][c] + row[2][c]);
     };
     const int cz0 = blockIdx.z * PZR, cz1 = min(gc.nz, cz0 + PZR);
     T Pm[3];
@@ -1006,7 +1003,24 @@ __global__ void __launch_bounds__(256)
             }
     };
     // Fine layer fz from the plane values P at the cell's coarse corners.
+    // All loads of a fine layer are issued before any is used (the flag does not
+    // guard them: vectors hold 0 at unused nodes), so they overlap in flight.
     auto emit = [&](int fz, const T (&P)[2][2][3]) {
+        T rr[2][2][3], dd[2][2][3];
+        uint8_t ff[2][2];
+#pragma unroll
+        for (int jy = 0; jy < 2; ++jy)
+#pragma unroll
+            for (int jx = 0; jx < 2; ++jx) {
+                const bool ex = (jx == 0 || hx) && (jy == 0 || hy);
+                const int64_t s = ex ? gf.store(2 * cx + jx, 2 * cy + jy, fz) : 0;
+                ff[jy][jx] = ex ? flags[s] : (uint8_t)0;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    rr[jy][jx][c] = ex ? rf[3 * s + c] : T(0);
+                    dd[jy][jx][c] = ex ? dinv[3 * s + c] : T(0);
+                }
+            }
 #pragma unroll
         for (int jy = 0; jy < 2; ++jy) {
             if (jy && !hy) continue;
@@ -1014,21 +1028,19 @@ __global__ void __launch_bounds__(256)
             for (int jx = 0; jx < 2; ++jx) {
                 if (jx && !hx) continue;
                 const int64_t s = gf.store(2 * cx + jx, 2 * cy + jy, fz);
-                const uint8_t fl = flags[s];
-                T out[3] = {T(0), T(0), T(0)}, r[3] = {T(0), T(0), T(0)};
-                if (fl & FLAG_USED) {
+                const uint8_t fl = ff[jy][jx];
+                const bool used = (fl & FLAG_USED) != 0;
+                const bool zero = !used || (maskFixed && (fl & FLAG_FIXED));
+                T out[3], r[3];
 #pragma unroll
-                    for (int c = 0; c < 3; ++c) {
-                        const T a0 = jx ? half * (P[0][0][c] + P[0][1][c]) : P[0][0][c];
-                        const T a1 = jx ? half * (P[1][0][c] + P[1][1][c]) : P[1][0][c];
-                        const T pv = jy ? half * (a0 + a1) : a0;
-                        r[c] = rf[3 * s + c];
-                        out[c] = pv + cf * dinv[3 * s + c] * r[c];
-                    }
-                    if (maskFixed && (fl & FLAG_FIXED)) out[0] = out[1] = out[2] = T(0);
+                for (int c = 0; c < 3; ++c) {
+                    const T a0 = jx ? half * (P[0][0][c] + P[0][1][c]) : P[0][0][c];
+                    const T a1 = jx ? half * (P[1][0][c] + P[1][1][c]) : P[1][0][c];
+                    const T pv = jy ? half * (a0 + a1) : a0;
+                    r[c] = used ? rr[jy][jx][c] : T(0);
+                    out[c] = zero ? T(0) : pv + cf * dd[jy][jx][c] * r[c];
+                    zf[3 * s + c] = out[c];
                 }
-#pragma unroll
-                for (int c = 0; c < 3; ++c) zf[3 * s + c] = out[c];
                 if (epi != EPI_NONE) {
 #pragma unroll
                     for (int c = 0; c < 3; ++c) {
@@ -1258,8 +1270,9 @@ __global__ void kGatherCompressed(int64_t nn, const int32_t* __restrict__ store,
 
 // One parity colour of the coarsest-matrix assembly: same-colour elements share
 // no node, so plain += is race-free and the summation order is fixed.
+template <typename T>
 __global__ void kAssembleCoarse(Grid g, const float* __restrict__ E, const int32_t* __restrict__ freeNode,
-                                const Kd<double> ke, double scale, double* __restrict__ K, int64_t n, int color) {
+                                const Kd<double> ke, double scale, T* __restrict__ K, int64_t n, int color) {
     const int hx = (g.ex + 1 - (color & 1)) / 2, hy = (g.ey + 1 - ((color >> 1) & 1)) / 2;
     const int64_t e = blockIdx.x;
     const int ix = (int)(e % hx), iy = (int)((e / hx) % hy), iz = (int)(e / ((int64_t)hx * hy));
@@ -1273,11 +1286,12 @@ __global__ void kAssembleCoarse(Grid g, const float* __restrict__ E, const int32
         const int32_t na = freeNode[g.store(x + (a & 1), y + ((a >> 1) & 1), z + (a >> 2))];
         const int32_t nb = freeNode[g.store(x + (b & 1), y + ((b >> 1) & 1), z + (b >> 2))];
         if (na < 0 || nb < 0) continue;
-        K[(3 * (int64_t)na + ci) * n + 3 * (int64_t)nb + cj] += scale * (double)Ee * ke.v[ent];
+        K[(3 * (int64_t)na + ci) * n + 3 * (int64_t)nb + cj] += (T)(scale * (double)Ee * ke.v[ent]);
     }
 }
 
-__global__ void kSymmetrize(double* K, int64_t n) {
+template <typename T>
+__global__ void kSymmetrize(T* K, int64_t n) {
     // Column-major lower triangle (cuSOLVER) == row-major upper triangle: copy it down.
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n * n; i += (int64_t)gridDim.x * blockDim.x) {
         const int64_t r = i / n, c = i % n;
@@ -1473,8 +1487,9 @@ int launchGatherCompressed(cudaStream_t s, int64_t nn, const int32_t* store, con
     return 1;
 }
 
+template <typename T>
 int launchAssembleCoarse(cudaStream_t s, const Grid& g, const float* E, const int32_t* freeNode, const double* Ke,
-                         double scale, double* K, int64_t n) {
+                         double scale, T* K, int64_t n) {
     Kd<double> k;
     for (int i = 0; i < 576; ++i) k.v[i] = Ke[i];
     int launches = 0;
@@ -1483,14 +1498,15 @@ int launchAssembleCoarse(cudaStream_t s, const Grid& g, const float* E, const in
                   hz = (g.ez + 1 - (color >> 2)) / 2;
         const int64_t ne = (int64_t)hx * hy * hz;
         if (ne <= 0) continue;
-        kAssembleCoarse<<<(unsigned)ne, 64, 0, s>>>(g, E, freeNode, k, scale, K, n, color);
+        kAssembleCoarse<T><<<(unsigned)ne, 64, 0, s>>>(g, E, freeNode, k, scale, K, n, color);
         ++launches;
     }
     return launches;
 }
 
-int launchSymmetrizeLowerToFull(cudaStream_t s, double* K, int64_t n) {
-    kSymmetrize<<<flatBlocks(n * n), NT, 0, s>>>(K, n);
+template <typename T>
+int launchSymmetrizeLowerToFull(cudaStream_t s, T* K, int64_t n) {
+    kSymmetrize<T><<<flatBlocks(n * n), NT, 0, s>>>(K, n);
     return 1;
 }
 
@@ -1584,7 +1600,10 @@ cudaError_t launchMatvecNoAlloc(cudaStream_t s, const MatvecArgs<double>& a, boo
     template int launchDots<T>(const LaunchCtx&, int64_t, const T*, const T*, const T*, const T*, int, int);         \
     template int launchFill<T>(cudaStream_t, int64_t, T*, T);                                                        \
     template int launchScatterCompressed<T>(cudaStream_t, int64_t, const int32_t*, const double*, T*);               \
-    template int launchGatherCompressed<T>(cudaStream_t, int64_t, const int32_t*, const T*, double*);
+    template int launchGatherCompressed<T>(cudaStream_t, int64_t, const int32_t*, const T*, double*);               \
+    template int launchAssembleCoarse<T>(cudaStream_t, const Grid&, const float*, const int32_t*, const double*,     \
+                                         double, T*, int64_t);                                                       \
+    template int launchSymmetrizeLowerToFull<T>(cudaStream_t, T*, int64_t);
 INST_T(double)
 INST_T(float)
 template int launchUpdateXR<double, double>(const LaunchCtx&, int64_t, double*, double*, const double*, const double*);

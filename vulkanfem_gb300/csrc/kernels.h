@@ -149,9 +149,11 @@ template <typename T>
 int launchGatherCompressed(cudaStream_t s, int64_t nnodes, const int32_t* nodeStore, const T* dense, double* comp);
 
 // Coarsest-matrix assembly (dense, free DOFs only), one parity colour per launch.
+template <typename T>
 int launchAssembleCoarse(cudaStream_t s, const Grid& g, const float* E, const int32_t* freeNode, const double* Ke,
-                         double scale, double* K, int64_t n);
-int launchSymmetrizeLowerToFull(cudaStream_t s, double* K, int64_t n);
+                         double scale, T* K, int64_t n);
+template <typename T>
+int launchSymmetrizeLowerToFull(cudaStream_t s, T* K, int64_t n);
 
 // Solver scalar initialisation (device side, so it can live in a graph).
 int launchInitScalars(cudaStream_t s, Scalars* S, double tol, long long maxIter, int flexible, int mixed,

@@ -1,30 +1,7 @@
-// setup.cpp -- host-side set-up of the voxel multigrid hierarchy.
-//
-// Restates assembleSystemMatrix (src/FEM.cpp:157-517 of the reference) on dense
-// structured grids instead of std::map node sets.  Every quantity the reference
-// builds has a structured equivalent here:
-//   * EnlistUsedElements + compressed numbering (FEM.cpp:66-100,179-186): a node
-//     is used when a filled voxel touches it; compressed ids follow linear order,
-//     which is the storage order of the dense node grid;
-//   * coarse elements (FEM.cpp:274-283): a coarse element is used when any of its
-//     children is used; dims are ceil-halved (ceil-quartered for the skipped
-//     first level, FEM.cpp:266-272);
-//   * restriction mapping + coefficients W = 1/multiplicity (FEM.cpp:340-362,400):
-//     every coarse element whose bounding stencil holds fine node f also has as
-//     corners all coarse nodes C with |f - d*C| < d, so the reference's
-//     sum over elements of R[f,C] W[f] equals the plain trilinear weight of
-//     (f - d*C); the kernels therefore apply full weighting with no tables;
-//   * fixed nodes per level (FEM.cpp:402-460): restricting the 0/1 indicator and
-//     keeping non-zeros is a dilation: C is fixed when any fixed fine node lies
-//     within |f - d*C| < d;
-//   * inverse diagonals (FEM.cpp:105-151,463): full coarse elements contribute
-//     2^(l+skip) diag(Ke); partially filled ones contribute the diagonal of the
-//     Galerkin matrix sum_children 2^(l-1) R^T Ke_child R (FEM.cpp:364-395),
-//     accumulated child by child from a per-child table;
-//   * early stop when the (ceil-halved) level dims reach <= 2 (FEM.cpp:465-470).
-// Extension with no reference counterpart: a per-voxel modulus E.  Coarse
-// elements carry the mean E of their used children; with E == 1 everything
-// reduces to the reference.
+// setup.cpp -- host-side pieces of the set-up: the element stiffness and its
+// Walsh-basis factorisation, the per-child Galerkin diagonal tables, and the
+// plan of the level grids.  The per-node hierarchy itself is built on the
+// device (setup_gpu.cu).
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -122,13 +99,14 @@ vfem_status prepareKe(const double* KeIn, KeData& k) {
 }
 
 namespace {
-
 inline double tri1(int a, int b, int div) { return b == 0 ? double(div - a) / div : double(a) / div; }
+
+}  // namespace
 
 // Per-child diagonal of R_DOF^T (Ke at child ch) R_DOF (RestrictionOperator.hpp:246-708
 // as the trilinear tensor product; child placement of RestrictionOperator.hpp:6-84).
 void childDiagTable(const double* Ke, int div, std::vector<double>& tab) {
-    int nch = div * div * div, n = div + 1;
+    int nch = div * div * div;
     tab.assign((size_t)nch * 24, 0.0);
     for (int ch = 0; ch < nch; ++ch) {
         int cx = ch % div, cy = (ch / div) % div, cz = ch / (div * div);
@@ -138,7 +116,6 @@ void childDiagTable(const double* Ke, int div, std::vector<double>& tab) {
             double r[8];
             for (int a = 0; a < 8; ++a) {
                 int fx = cx + (a & 1), fy = cy + ((a >> 1) & 1), fz = cz + ((a >> 2) & 1);
-                (void)n;
                 r[a] = tri1(fx, bx, div) * tri1(fy, by, div) * tri1(fz, bz, div);
             }
             double s = 0;
@@ -155,58 +132,8 @@ void initGrid(Grid& g, int ex, int ey, int ez) {
     g.nnode = (int64_t)g.nx * g.ny * g.nz;
 }
 
-// Node flags from the element field; compressed numbering in storage order.
-void markNodes(HostLevel& l) {
-    const Grid& g = l.g;
-    l.flags.assign(g.nnode, 0);
-    l.nelem = 0;
-    for (int z = 0; z < g.ez; ++z)
-        for (int y = 0; y < g.ey; ++y)
-            for (int x = 0; x < g.ex; ++x) {
-                if (l.E[g.store(x, y, z)] == 0.f) continue;
-                ++l.nelem;
-                for (int d = 0; d < 8; ++d) l.flags[g.store(x + (d & 1), y + ((d >> 1) & 1), z + (d >> 2))] |= FLAG_USED;
-            }
-    l.nodeStore.clear();
-    for (int64_t s = 0; s < g.nnode; ++s)
-        if (l.flags[s] & FLAG_USED) l.nodeStore.push_back((int32_t)s);
-}
-
-void fixedIdsFromFlags(HostLevel& l) {
-    l.fixedIds.clear();
-    for (size_t i = 0; i < l.nodeStore.size(); ++i)
-        if (l.flags[l.nodeStore[i]] & FLAG_FIXED) l.fixedIds.push_back((int64_t)i);
-}
-
-void invert(std::vector<double>& d, const std::vector<uint8_t>& flags) {
-    for (size_t s = 0; s < flags.size(); ++s)
-        for (int c = 0; c < 3; ++c) {
-            double& v = d[3 * s + c];
-            v = (flags[s] & FLAG_USED) ? 1.0 / v : 0.0;
-        }
-}
-
-// Diagonal of scale * sum_e Ef_e Ke over the elements touching each node.
-void rediscretisedDiag(const HostLevel& l, const std::vector<float>& Ef, const KeData& ke, std::vector<double>& d) {
-    const Grid& g = l.g;
-    d.assign(3 * g.nnode, 0.0);
-    for (int z = 0; z < g.ez; ++z)
-        for (int y = 0; y < g.ey; ++y)
-            for (int x = 0; x < g.ex; ++x) {
-                float E = Ef[g.store(x, y, z)];
-                if (E == 0.f) continue;
-                for (int a = 0; a < 8; ++a) {
-                    int64_t s = g.store(x + (a & 1), y + ((a >> 1) & 1), z + (a >> 2));
-                    for (int c = 0; c < 3; ++c) d[3 * s + c] += l.scale * (double)E * ke.diag[3 * a + c];
-                }
-            }
-}
-
-}  // namespace
-
-vfem_status buildHierarchy(const uint8_t* vox, int nx, int ny, int nz, const float* Ein,
-                           const int64_t* fixed, int64_t nfixed, int numLevels, int skip,
-                           const KeData& ke, Hierarchy& H, std::string& err) {
+vfem_status planLevels(int nx, int ny, int nz, int numLevels, int skip, std::vector<LevelPlan>& out,
+                       std::string& err) {
     if (nx < 1 || ny < 1 || nz < 1 || numLevels < 1 || skip < 0 || skip > 1) {
         err = "invalid dimensions, level count or skip";
         return VFEM_ERR_INVALID_ARGUMENT;
@@ -215,132 +142,23 @@ vfem_status buildHierarchy(const uint8_t* vox, int nx, int ny, int nz, const flo
         err = "grid too large for 32-bit DOF indexing";
         return VFEM_ERR_INVALID_ARGUMENT;
     }
-    H.L.clear();
-    H.skip = skip;
-    H.L.emplace_back();
-    HostLevel& l0 = H.L[0];
+    out.clear();
+    LevelPlan l0;
     initGrid(l0.g, nx, ny, nz);
-    l0.divider = 1;
+    l0.div = 1;
     l0.scale = 1.0;
-    l0.E.assign(l0.g.nnode, 0.f);
-    int64_t filled = 0;
-    for (int z = 0; z < nz; ++z)
-        for (int y = 0; y < ny; ++y)
-            for (int x = 0; x < nx; ++x) {
-                int64_t v = ((int64_t)z * ny + y) * nx + x;
-                if (vox[v] == 1) {
-                    float e = Ein ? Ein[v] : 1.f;
-                    if (!(e > 0.f) || !std::isfinite(e)) {
-                        err = "non-positive or non-finite modulus on a filled voxel";
-                        return VFEM_ERR_INVALID_ARGUMENT;
-                    }
-                    l0.E[l0.g.store(x, y, z)] = e;
-                    ++filled;
-                } else if (vox[v] != 0) {
-                    err = "voxel values must be 0 or 1";
-                    return VFEM_ERR_INVALID_ARGUMENT;
-                }
-            }
-    if (filled == 0) {
-        err = "no filled voxel";
-        return VFEM_ERR_EMPTY;
-    }
-    markNodes(l0);
-    int64_t nused = (int64_t)l0.nodeStore.size();
-    for (int64_t i = 0; i < nfixed; ++i) {
-        if (fixed[i] < 0 || fixed[i] >= nused) {
-            err = "fixed node id out of range";
-            return VFEM_ERR_INVALID_ARGUMENT;
-        }
-        l0.flags[l0.nodeStore[fixed[i]]] |= FLAG_FIXED;
-    }
-    fixedIdsFromFlags(l0);
-    l0.Ev = l0.E;
-    rediscretisedDiag(l0, l0.E, ke, l0.dinv);
-    l0.dinvRedisc = l0.dinv;
-    invert(l0.dinv, l0.flags);
-    invert(l0.dinvRedisc, l0.flags);
-
-    std::vector<double> tab2, tab4;
-    childDiagTable(ke.Ke, 2, tab2);
-    childDiagTable(ke.Ke, 4, tab4);
+    out.push_back(l0);
+    // Early stop once the (ceil-halved) reference dims reach <= 2 (FEM.cpp:465-470).
     int refDims[3] = {nx, ny, nz};
     for (int i = 1; i < numLevels; ++i) {
-        const HostLevel& f = H.L[i - 1];
-        int div = (i == 1 && skip > 0) ? (1 << (skip + 1)) : 2;
-        HostLevel c;
-        initGrid(c.g, (f.g.ex + div - 1) / div, (f.g.ey + div - 1) / div, (f.g.ez + div - 1) / div);
-        c.divider = div;
+        const Grid& f = out.back().g;
+        LevelPlan c;
+        c.div = (i == 1 && skip > 0) ? (1 << (skip + 1)) : 2;
+        initGrid(c.g, (f.ex + c.div - 1) / c.div, (f.ey + c.div - 1) / c.div, (f.ez + c.div - 1) / c.div);
         c.scale = std::pow(2.0, i + skip);
-        int nch = div * div * div;
-        const std::vector<double>& tab = div == 4 ? tab4 : tab2;
-        double childScale = std::pow(2.0, i - 1);
-        c.E.assign(c.g.nnode, 0.f);
-        c.Ev.assign(c.g.nnode, 0.f);
-        c.dinv.assign(3 * c.g.nnode, 0.0);
-        // Coarse elements: used children, mean modulus, diagonal contributions.
-        for (int z = 0; z < c.g.ez; ++z)
-            for (int y = 0; y < c.g.ey; ++y)
-                for (int x = 0; x < c.g.ex; ++x) {
-                    double sumE = 0, sumEv = 0;
-                    int cnt = 0;
-                    double part[24] = {};
-                    for (int ch = 0; ch < nch; ++ch) {
-                        int fx = x * div + ch % div, fy = y * div + (ch / div) % div, fz = z * div + ch / (div * div);
-                        if (fx >= f.g.ex || fy >= f.g.ey || fz >= f.g.ez) continue;
-                        float Ef = f.E[f.g.store(fx, fy, fz)];
-                        if (Ef == 0.f) continue;
-                        ++cnt;
-                        sumE += Ef;
-                        sumEv += f.Ev[f.g.store(fx, fy, fz)];
-                        for (int k = 0; k < 24; ++k) part[k] += childScale * (double)Ef * tab[(size_t)ch * 24 + k];
-                    }
-                    if (!cnt) continue;
-                    float Ec = (float)(sumE / cnt);
-                    c.E[c.g.store(x, y, z)] = Ec;
-                    c.Ev[c.g.store(x, y, z)] = (float)(sumEv / nch);
-                    bool full = cnt == nch;
-                    for (int a = 0; a < 8; ++a) {
-                        int64_t s = c.g.store(x + (a & 1), y + ((a >> 1) & 1), z + (a >> 2));
-                        for (int cc = 0; cc < 3; ++cc) {
-                            int k = 3 * a + cc;
-                            c.dinv[3 * s + cc] += full ? c.scale * (double)Ec * ke.diag[k] : part[k];
-                        }
-                    }
-                }
-        markNodes(c);
-        // Fixed dilation.
-        int reach = div - 1;
-        for (int z = 0; z < c.g.nz; ++z)
-            for (int y = 0; y < c.g.ny; ++y)
-                for (int x = 0; x < c.g.nx; ++x) {
-                    bool fx_ = false;
-                    for (int dz = -reach; dz <= reach && !fx_; ++dz)
-                        for (int dy = -reach; dy <= reach && !fx_; ++dy)
-                            for (int dx = -reach; dx <= reach && !fx_; ++dx) {
-                                int X = x * div + dx, Y = y * div + dy, Z = z * div + dz;
-                                if (X < 0 || Y < 0 || Z < 0 || X >= f.g.nx || Y >= f.g.ny || Z >= f.g.nz) continue;
-                                if (f.flags[f.g.store(X, Y, Z)] & FLAG_FIXED) fx_ = true;
-                            }
-                    if (fx_) c.flags[c.g.store(x, y, z)] |= FLAG_FIXED;
-                }
-        fixedIdsFromFlags(c);
-        rediscretisedDiag(c, c.Ev, ke, c.dinvRedisc);
-        invert(c.dinv, c.flags);
-        invert(c.dinvRedisc, c.flags);
-        H.L.push_back(std::move(c));
+        out.push_back(c);
         for (int d = 0; d < 3; ++d) refDims[d] = refDims[d] / 2 + refDims[d] % 2;
         if (refDims[0] <= 2 || refDims[1] <= 2 || refDims[2] <= 2) break;
-    }
-    // Coarsest free DOFs (FEM.cpp:473-496), in compressed (storage) order.
-    const HostLevel& lc = H.L.back();
-    H.coarseFreeDof.clear();
-    H.coarseFreeNode.assign(lc.g.nnode, -1);
-    int32_t nf = 0;
-    for (int32_t s : lc.nodeStore) {
-        if (lc.flags[s] & FLAG_FIXED) continue;
-        H.coarseFreeNode[s] = nf++;
-        for (int cc = 0; cc < 3; ++cc) H.coarseFreeDof.push_back(3 * s + cc);
     }
     return VFEM_OK;
 }

@@ -48,34 +48,21 @@ struct KeData {
 extern const int kPatRow[45];
 extern const int kPatCol[45];
 
-struct HostLevel {
+// One level of the hierarchy as planned on the host (setup.cpp); its per-node
+// data is built on the device (setup_gpu.cu).
+struct LevelPlan {
     Grid g;
-    int divider = 2;               // coarsening factor from the previous level
-    double scale = 1.0;            // operator multiplier 2^(level+skip)
-    std::vector<float> E;          // per element (lower-corner storage index), 0 = empty
-    std::vector<float> Ev;         // multiplicative-cycle modulus: volume average of the children
-                                   // (empty children count as 0); equals E on the finest level
-    std::vector<uint8_t> flags;    // per node
-    std::vector<double> dinv;      // 3 per node: reference inverse diagonal (Galerkin for partial elements)
-    std::vector<double> dinvRedisc;// 3 per node: inverse diagonal of the rediscretised operator
-    std::vector<int32_t> nodeStore;// compressed id -> storage index
-    std::vector<int64_t> fixedIds; // compressed ids of fixed nodes, sorted
-    int64_t nelem = 0;
+    int div = 2;         // coarsening factor from the previous level (1 on level 0)
+    double scale = 1.0;  // operator multiplier 2^(level+skip)
 };
 
-struct Hierarchy {
-    std::vector<HostLevel> L;
-    int skip = 0;
-    // coarsest level
-    std::vector<int32_t> coarseFreeDof;   // storage DOF index (3*s + c) of each free coarse DOF
-    std::vector<int32_t> coarseFreeNode;  // storage node -> free node id, -1 otherwise
-};
-
-// Host set-up (setup.cpp).
+// Host set-up pieces (setup.cpp).
 vfem_status prepareKe(const double* KeIn, KeData& out);
-vfem_status buildHierarchy(const uint8_t* vox, int nx, int ny, int nz, const float* E,
-                           const int64_t* fixed, int64_t nfixed, int numLevels, int skip,
-                           const KeData& ke, Hierarchy& H, std::string& err);
+vfem_status planLevels(int nx, int ny, int nz, int numLevels, int skip, std::vector<LevelPlan>& out,
+                       std::string& err);
+// Per-child diagonal of R^T Ke_child R for the div^3 children of a coarse element (div^3 x 24).
+void childDiagTable(const double* Ke, int div, std::vector<double>& tab);
+void initGrid(Grid& g, int ex, int ey, int ez);
 void hex8Stiffness(double E, double nu, double* Ke);
 
 }  // namespace vfem
