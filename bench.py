@@ -159,6 +159,14 @@ class Dist:
             self.dist.destroy_process_group()
 
 
+def replica_throughput(dist, seconds, dof_iterations):
+    """Whole-job MDOF/s of independent replicas: all ranks' DOF x iterations over
+    the slowest rank's time.  Returns (MDOF/s, max seconds)."""
+    tmax, = dist.reduce([float(seconds)], "max")
+    work, = dist.reduce([float(dof_iterations)], "sum")
+    return work / tmax / 1e6, tmax
+
+
 def algorithmic_bytes(kind, g0, g1, s):
     """Algorithmic bytes per launch on the finest level.  N = grid nodes, Ne = voxels
     (dense-grid model): matvec 6sN + Ne/8 + 4Ne + N/8 (x in, y out, occupancy bits,
@@ -244,6 +252,9 @@ def main():
     ap.add_argument("--cpu-iters", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-reps", type=int, default=20)
+    ap.add_argument("--kernels-only", action="store_true",
+                    help="profiling case for ncu: set-up, a 4-iteration solve and one launch of each kernel class; "
+                         "prints the kernel-class times and no bench line")
     args = ap.parse_args()
 
     ws, rank, local = dist_env()
@@ -258,6 +269,13 @@ def main():
         return
 
     from vulkanfem_gb300 import api, domains
+    if args.kernels_only:
+        A = api.assembleSystemMatrix(dom.voxels, domains.hex8_stiffness(), dom.fixed, dom.num_levels, 0, E=dom.E)
+        A.set_loads(dom.load_nodes, dom.load_values)
+        _, st = A.solve_device(allow_not_converged=True, max_iter=4, **SOLVERS[args.solver])
+        print(json.dumps({"kernels_only": args.workload, "iterations": st["iterations"],
+                          "kernel_ms": api.profile_kernels(A, 1)}), flush=True)
+        return
     dist = Dist(ws)
     ke = domains.hex8_stiffness()
     t0 = time.perf_counter()
@@ -283,9 +301,7 @@ def main():
     dist.barrier()
     dev_s = sum(st["solve_ms"] for st in stats) / 1e3
     iters = sum(st["iterations"] for st in stats)
-    tmax, = dist.reduce([dev_s], "max")
-    work, = dist.reduce([float(dof * iters)], "sum")
-    value = work / tmax / 1e6
+    value, tmax = replica_throughput(dist, dev_s, dof * iters)
 
     # ---- end to end through the C ABI with host buffers (e2e)
     f = dom.load_vector()
@@ -298,9 +314,7 @@ def main():
         u, st = A.solve(f, **sopts)
         e_it += st["iterations"]
     e_s = time.perf_counter() - e0
-    emax, = dist.reduce([e_s], "max")
-    ework, = dist.reduce([float(dof * e_it)], "sum")
-    e2e = ework / emax / 1e6
+    e2e, _ = replica_throughput(dist, e_s, dof * e_it)
 
     # ---- comparison solver (plain FP64 MG-PCG on the same GPU)
     comp = None

@@ -84,16 +84,18 @@ struct vfem_problem {
     // coarsest dense inverse
     int64_t nc = 0;
     int32_t* freeDof = nullptr;
-    // Coarsest dense inverses, built on first use (ensureCoarse): FP64 for the
-    // FP64 solver and preconditioner, FP32 for the mixed one; V = the
+    // Coarsest dense inverses, built on first use (ensureCoarse): FP64 (full
+    // n x n) for the FP64 solver and preconditioner, FP32 (the packed lower block
+    // triangle of 64 x 64 tiles, launchPackSym) for the mixed one; V = the
     // multiplicative cycle's operator (volume-averaged modulus).
     double* Kinv64 = nullptr;
     float* Kinv32 = nullptr;
     double* KinvV64 = nullptr;
     float* KinvV32 = nullptr;
     int32_t* dFreeNode = nullptr;  // coarsest storage node -> free node id (assembly)
-    double* cb64 = nullptr;
+    double* cb64 = nullptr;        // gathered coarse right-hand side, coarseBlocks(nc) * 64 (zero tail)
     float* cb32 = nullptr;
+    double* cpart = nullptr;       // per-tile partial products, 128 per tile (used as float or double)
     // reductions / scalars
     Scalars* S = nullptr;
     Scalars* hS = nullptr;
@@ -154,7 +156,7 @@ void freeProblem(vfem_problem* p) {
     cudaFree(p->f64); cudaFree(p->x64); cudaFree(p->p64); cudaFree(p->Ap64); cudaFree(p->p32); cudaFree(p->Ap32);
     cudaFree(p->x32);
     cudaFree(p->freeDof); cudaFree(p->Kinv64); cudaFree(p->Kinv32); cudaFree(p->cb64); cudaFree(p->cb32);
-    cudaFree(p->KinvV64); cudaFree(p->KinvV32); cudaFree(p->dFreeNode);
+    cudaFree(p->KinvV64); cudaFree(p->KinvV32); cudaFree(p->dFreeNode); cudaFree(p->cpart);
     cudaFree(p->S); cudaFree(p->rb.partials); cudaFree(p->rb.ticket); cudaFree(p->dComp);
     if (p->hS) cudaFreeHost(p->hS);
     if (p->hIn) cudaFreeHost(p->hIn);
@@ -193,8 +195,9 @@ vfem_status buildCoarse(vfem_problem* p) {
     if (n == 0) return VFEM_OK;
     CK(upload(&p->freeDof, p->coarseFreeDof));
     CK(upload(&p->dFreeNode, p->coarseFreeNode));
-    CK(dalloc(&p->cb64, n));
-    CK(dalloc(&p->cb32, n));
+    CK(dalloc(&p->cb64, coarseBlocks(n) * CT));
+    CK(dalloc(&p->cb32, coarseBlocks(n) * CT));
+    CK(dalloc(&p->cpart, coarseTiles(n) * 2 * CT));
     return VFEM_OK;
 }
 
@@ -312,23 +315,35 @@ vfem_status ensureCoarse(vfem_problem* p, bool vcycle) {
     if (p->nc == 0) return VFEM_OK;
     T*& K = kinvSlot<T>(p, vcycle);
     if (K) return VFEM_OK;
-    T* buf = nullptr;
-    CK(dalloc(&buf, p->nc * p->nc));
+    // FP64: the full matrix (applied by a one-FMA-per-value GEMV); FP32: packed tiles.
+    const bool packedForm = std::is_same<T, float>::value;
+    const int64_t n = p->nc, stored = packedForm ? coarseTiles(n) * CT * CT : n * n;
+    T* out = nullptr;
+    CK(dalloc(&out, stored));
+    T* full = out;
+    if (packedForm && dalloc(&full, n * n) != cudaSuccess) {
+        cudaFree(out);
+        return fail(VFEM_ERR_OUT_OF_MEMORY, "coarse inverse workspace");
+    }
     const DevLevel& dc = p->L.back();
-    vfem_status st = invertCoarse<T>(p, vcycle ? dc.Ev : dc.E, dc.scale, buf);
-    if (st == VFEM_ERR_SINGULAR && std::is_same<T, float>::value) {
+    vfem_status st = invertCoarse<T>(p, vcycle ? dc.Ev : dc.E, dc.scale, full);
+    if (st == VFEM_OK && packedForm) {
+        p->launches += launchPackSym<T>(p->stream, full, n, out);
+        if (cudaStreamSynchronize(p->stream) != cudaSuccess) st = fail(VFEM_ERR_CUDA, "coarse inverse packing");
+    } else if (st == VFEM_ERR_SINGULAR && packedForm) {
         st = ensureCoarse<double>(p, vcycle);
         if (st == VFEM_OK) {
-            launchConvert<double, T>(p->stream, p->nc * p->nc, kinvSlot<double>(p, vcycle), buf);
-            ++p->launches;
+            launchConvert<double, T>(p->stream, n * n, kinvSlot<double>(p, vcycle), full);
+            p->launches += 1 + launchPackSym<T>(p->stream, full, n, out);
             if (cudaStreamSynchronize(p->stream) != cudaSuccess) st = fail(VFEM_ERR_CUDA, "coarse inverse copy");
         }
     }
+    if (full != out) cudaFree(full);
     if (st != VFEM_OK) {
-        cudaFree(buf);
+        cudaFree(out);
         return st;
     }
-    K = buf;
+    K = out;
     return VFEM_OK;
 }
 
@@ -615,7 +630,7 @@ int vcycle(vfem_problem* p, const vfem_options& o, int lv, T* r, T* z, T** outZ,
     if (lv == L - 1) {
         // Coarsest: exact dense-inverse solve on the free DOFs; fixed and unused DOFs stay 0.
         n += launchCoarseSolve<T>(c, o.mg_mode == VFEM_MG_VCYCLE ? kinvV<T>(p) : kinv<T>(p), p->nc, p->freeDof, r,
-                                  cbuf<T>(p), z, 1);
+                                  cbuf<T>(p), reinterpret_cast<T*>(p->cpart), z, 1);
         if (lv == 0 && epi != EPI_NONE) n += launchDots<T>(c, l.nvec(), r, z, aux ? z : nullptr, aux, epi, 1);
         *outZ = z;
         return n;
@@ -1145,11 +1160,13 @@ vfem_status vfem_profile_kernels(vfem_problem* p, int32_t reps, double* ms) {
                     return launchUpdateP<float>(c, n, p->p32, l0.z32, 0);
                 case VFEM_K_COARSE_FP64: {
                     DevLevel& lc = p->L.back();
-                    return launchCoarseSolve<double>(c, p->Kinv64, p->nc, p->freeDof, lc.r64, p->cb64, lc.z64, 1);
+                    return launchCoarseSolve<double>(c, p->Kinv64, p->nc, p->freeDof, lc.r64, p->cb64, p->cpart,
+                                                     lc.z64, 1);
                 }
                 case VFEM_K_COARSE_FP32: {
                     DevLevel& lc = p->L.back();
-                    return launchCoarseSolve<float>(c, p->Kinv32, p->nc, p->freeDof, lc.r32, p->cb32, lc.z32, 1);
+                    return launchCoarseSolve<float>(c, p->Kinv32, p->nc, p->freeDof, lc.r32, p->cb32,
+                                                    reinterpret_cast<float*>(p->cpart), lc.z32, 1);
                 }
                 default: {
                     MatvecArgs<double> a = mvArgs<double>(p, 0, p->x64, nullptr, MV_RESID);

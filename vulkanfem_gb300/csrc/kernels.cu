@@ -9,8 +9,9 @@
 //                    full weighting on the dense grid, one thread per coarse node.
 //   kProlongSmooth   Interpolate.comp + PreSmoothAndAXPY.comp + Smooth.comp
 //                    (MultigridPreconditioner.hpp:110-155,176-181), fixed mask and r.z fused.
-//   kCoarseGather/kGemv  the coarsest SimplicialLDLT solve (MultigridPreconditioner.hpp:174-175)
-//                    as a dense inverse applied on the device.
+//   kCoarseGather/kSymTile/kSymReduce  the coarsest SimplicialLDLT solve
+//                    (MultigridPreconditioner.hpp:174-175) as a dense symmetric
+//                    inverse, stored as half its tiles, applied on the device.
 //   kUpdateXR        ConjugateGradient_1.comp + VecDotVec.comp (r.r).
 //   kUpdateP         ConjugateGradient_2.comp.
 // Reductions are deterministic: block partials in a fixed grid, summed in a
@@ -26,7 +27,7 @@ namespace vfem {
 
 namespace {
 
-constexpr int MV_TX = 32, MV_TY = 8, MV_ZC = 16;
+constexpr int MV_TX = 32, MV_TY = 8, MV_ZC = 32;  // z layers per product block (32: 5% faster than 16)
 constexpr int NT = 256;
 constexpr int PZ = 8;  // z nodes per thread in the per-node kernels
 
@@ -1119,23 +1120,6 @@ __global__ void kCoarseGather(int64_t n, const int32_t* __restrict__ freeDof, co
         b[i] = rc[freeDof[i]];
 }
 
-// y = Kinv b, one warp per row; results scattered to the coarse free DOFs.
-template <typename T>
-__global__ void __launch_bounds__(256) kGemv(const T* __restrict__ K, int64_t n, const T* __restrict__ b,
-                                             const int32_t* __restrict__ freeDof, T* __restrict__ zc,
-                                             const Scalars* S, int checkDone) {
-    if (checkDone && S->done) return;
-    const int lane = threadIdx.x & 31;
-    const int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    if (row >= n) return;
-    const T* k = K + row * n;
-    T acc = T(0);
-    for (int64_t j = lane; j < n; j += 32) acc = fma(k[j], b[j], acc);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (lane == 0) zc[freeDof[row]] = acc;
-}
-
 // 4-wide vector loads/stores of the flat vector kernels (float4; two double2).
 template <typename T>
 struct V4;
@@ -1160,6 +1144,136 @@ struct V4<double> {
         reinterpret_cast<double2*>(p)[1] = make_double2(v[2], v[3]);
     }
 };
+
+// y = Kinv b with the full inverse, one warp per row (FP64: the packed form below
+// needs two FMAs per stored value plus FP64 shuffle reductions, which GB300's
+// narrow FP64 pipe turns into 1.7x the time of this one-FMA-per-value form).
+__global__ void __launch_bounds__(256) kGemv64(const double* __restrict__ K, int64_t n, const double* __restrict__ b,
+                                               const int32_t* __restrict__ freeDof, double* __restrict__ zc,
+                                               const Scalars* S, int checkDone) {
+    if (checkDone && S->done) return;
+    const int lane = threadIdx.x & 31;
+    const int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (row >= n) return;
+    const double* k = K + row * n;
+    double acc = 0.0;
+    for (int64_t j = lane; j < n; j += 32) acc = fma(k[j], b[j], acc);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) zc[freeDof[row]] = acc;
+}
+
+// ---- coarsest solve: y = Kinv b with the symmetric inverse stored once.
+// Kinv is kept as the lower block triangle of 64 x 64 tiles (tile (I, J <= I) at
+// index I (I + 1) / 2 + J, row-major inside, zero-padded past n), half the bytes
+// of the full matrix.  kSymTile reads each tile once and writes its two partial
+// products, K_IJ b_J (for y_I) and K_IJ^T b_I (for y_J, off-diagonal tiles);
+// kSymReduce sums them per row block in a fixed order (deterministic, no atomics).
+__host__ __device__ inline int64_t symTileCount(int64_t nb) { return nb * (nb + 1) / 2; }
+// Tile index -> (I, J): FP32 square root, corrected exactly in integers (an FP64
+// square root per thread would run on GB300's narrow FP64 pipe).
+__device__ inline void symTileDecode(int64_t t, int64_t& I, int64_t& J) {
+    int64_t i = (int64_t)((sqrtf(8.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
+    while (i > 0 && i * (i + 1) / 2 > t) --i;
+    while ((i + 1) * (i + 2) / 2 <= t) ++i;
+    I = i;
+    J = t - i * (i + 1) / 2;
+}
+
+template <typename T>
+__global__ void kPackSym(const T* __restrict__ K, int64_t n, int64_t nb, T* __restrict__ tiles) {
+    const int64_t total = symTileCount(nb) * CT * CT;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        int64_t I, J;
+        symTileDecode(i / (CT * CT), I, J);
+        const int e = (int)(i % (CT * CT));
+        const int64_t row = I * CT + e / CT, col = J * CT + e % CT;
+        tiles[i] = (row < n && col < n) ? (T)K[row * n + col] : T(0);
+    }
+}
+
+// One tile per block: 16 x 16 threads, each a 4 x 4 sub-block (four 16-byte
+// row loads).  Row sums reduce over the 16 column groups by shuffles; column
+// sums over the two row groups of a warp by one shuffle, then over the 8
+// warps in shared memory.  part holds 2 x 64 values per tile.
+template <typename T>
+__global__ void __launch_bounds__(256) kSymTile(const T* __restrict__ tiles, const T* __restrict__ b,
+                                                T* __restrict__ part, const Scalars* S, int checkDone) {
+    if (checkDone && S->done) return;
+    __shared__ T colp[8][CT];
+    const int64_t t = blockIdx.x;
+    int64_t I, J;
+    symTileDecode(t, I, J);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int tc = lane & 15, tr = warp * 2 + (lane >> 4);
+    const T* K = tiles + t * (CT * CT);
+    T bJ[4], bI[4], rs[4], cs[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        bJ[j] = b[J * CT + 4 * tc + j];
+        bI[j] = b[I * CT + 4 * tr + j];
+        rs[j] = cs[j] = T(0);
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        T k[4];
+        V4<T>::ld(K + (4 * tr + i) * CT + 4 * tc, k);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            rs[i] = fma(k[j], bJ[j], rs[i]);
+            cs[j] = fma(k[j], bI[i], cs[j]);
+        }
+    }
+#pragma unroll
+    for (int o = 1; o < 16; o <<= 1)
+#pragma unroll
+        for (int i = 0; i < 4; ++i) rs[i] += __shfl_xor_sync(0xffffffffu, rs[i], o);
+    T* pt = part + t * (2 * CT);
+    if (tc == 0) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) pt[4 * tr + i] = rs[i];
+    }
+    const bool offDiag = I != J;
+    if (offDiag) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) cs[j] += __shfl_xor_sync(0xffffffffu, cs[j], 16);
+        if (lane < 16) {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) colp[warp][4 * tc + j] = cs[j];
+        }
+    }
+    __syncthreads();
+    if (offDiag && threadIdx.x < CT) {
+        T s = T(0);
+#pragma unroll
+        for (int w = 0; w < 8; ++w) s += colp[w][threadIdx.x];
+        pt[CT + threadIdx.x] = s;
+    }
+}
+
+// y_I = sum_{J <= I} (K_IJ b_J) + sum_{I' > I} (K_I'I^T b_I'); 16 groups of 64
+// threads split the tiles of row block I, then one group adds the 16 sums.
+template <typename T>
+__global__ void __launch_bounds__(1024) kSymReduce(const T* __restrict__ part, int64_t nb, int64_t n,
+                                                   const int32_t* __restrict__ freeDof, T* __restrict__ zc,
+                                                   const Scalars* S, int checkDone) {
+    if (checkDone && S->done) return;
+    __shared__ T red[16][CT];
+    const int64_t I = blockIdx.x;
+    const int r = threadIdx.x & (CT - 1), grp = threadIdx.x >> 6;
+    T s = T(0);
+    for (int64_t J = grp; J <= I; J += 16) s += part[(I * (I + 1) / 2 + J) * (2 * CT) + r];
+    for (int64_t Ip = I + 1 + grp; Ip < nb; Ip += 16) s += part[(Ip * (Ip + 1) / 2 + I) * (2 * CT) + CT + r];
+    red[grp][r] = s;
+    __syncthreads();
+    if (grp == 0) {
+        T y = T(0);
+#pragma unroll
+        for (int q = 0; q < 16; ++q) y += red[q][r];
+        const int64_t i = I * CT + r;
+        if (i < n) zc[freeDof[i]] = y;
+    }
+}
 
 // x += alpha p; r -= alpha Ap; r.r.  TX = double is the FP64 solution; TX = float
 // is the mixed-precision correction accumulated since the last flush.
@@ -1432,12 +1546,26 @@ int launchProlongAdd(const LaunchCtx& c, const Grid& gf, const Grid& gc, int div
 }
 
 template <typename T>
-int launchCoarseSolve(const LaunchCtx& c, const T* Kinv, int64_t n, const int32_t* freeDof, const T* rc, T* tmp, T* zc,
-                      int checkDone) {
+int launchCoarseSolve(const LaunchCtx& c, const T* Kinv, int64_t n, const int32_t* freeDof, const T* rc, T* tmp,
+                      T* part, T* zc, int checkDone) {
     if (n <= 0) return 0;
     kCoarseGather<T><<<(int)((n + 255) / 256), 256, 0, c.stream>>>(n, freeDof, rc, tmp, c.S, checkDone);
-    kGemv<T><<<(int)((n * 32 + 255) / 256), 256, 0, c.stream>>>(Kinv, n, tmp, freeDof, zc, c.S, checkDone);
-    return 2;
+    if constexpr (std::is_same<T, double>::value) {
+        kGemv64<<<(int)((n * 32 + 255) / 256), 256, 0, c.stream>>>(Kinv, n, tmp, freeDof, zc, c.S, checkDone);
+        return 2;
+    } else {
+        const int64_t nb = coarseBlocks(n);
+        kSymTile<T><<<(unsigned)symTileCount(nb), 256, 0, c.stream>>>(Kinv, tmp, part, c.S, checkDone);
+        kSymReduce<T><<<(unsigned)nb, 1024, 0, c.stream>>>(part, nb, n, freeDof, zc, c.S, checkDone);
+        return 3;
+    }
+}
+
+template <typename T>
+int launchPackSym(cudaStream_t s, const T* K, int64_t n, T* tiles) {
+    const int64_t nb = coarseBlocks(n);
+    kPackSym<T><<<flatBlocks(symTileCount(nb) * CT * CT), NT, 0, s>>>(K, n, nb, tiles);
+    return 1;
 }
 
 template <typename TX, typename TV>
@@ -1595,7 +1723,9 @@ cudaError_t launchMatvecNoAlloc(cudaStream_t s, const MatvecArgs<double>& a, boo
                                      int);                                                                           \
     template int launchProlongAdd<T>(const LaunchCtx&, const Grid&, const Grid&, int, const T*, const uint8_t*, T*,  \
                                      int);                                                                           \
-    template int launchCoarseSolve<T>(const LaunchCtx&, const T*, int64_t, const int32_t*, const T*, T*, T*, int);   \
+    template int launchCoarseSolve<T>(const LaunchCtx&, const T*, int64_t, const int32_t*, const T*, T*, T*, T*,     \
+                                      int);                                                                          \
+    template int launchPackSym<T>(cudaStream_t, const T*, int64_t, T*);                                              \
     template int launchUpdateP<T>(const LaunchCtx&, int64_t, T*, const T*, int);                                     \
     template int launchDots<T>(const LaunchCtx&, int64_t, const T*, const T*, const T*, const T*, int, int);         \
     template int launchFill<T>(cudaStream_t, int64_t, T*, T);                                                        \

@@ -117,10 +117,19 @@ template <typename T>
 int launchProlongAdd(const LaunchCtx& c, const Grid& gf, const Grid& gc, int div, const T* zc,
                      const uint8_t* flags, T* zf, int checkDone);
 
-// Coarsest level: zc[free] = Kinv * rc[free].
+// Coarsest level: zc[free] = Kinv * rc[free].  FP32: Kinv is the packed lower
+// block triangle of CT x CT tiles (launchPackSym), tmp holds coarseBlocks(n) * CT
+// values (zero past n), part 2 * CT values per tile.  FP64: Kinv is the full
+// n x n matrix (part unused).
+constexpr int CT = 64;
+inline int64_t coarseBlocks(int64_t n) { return (n + CT - 1) / CT; }
+inline int64_t coarseTiles(int64_t n) { return coarseBlocks(n) * (coarseBlocks(n) + 1) / 2; }
 template <typename T>
 int launchCoarseSolve(const LaunchCtx& c, const T* Kinv, int64_t n, const int32_t* freeDof, const T* rc, T* tmp,
-                      T* zc, int checkDone);
+                      T* part, T* zc, int checkDone);
+// Pack a full symmetric row-major n x n matrix into coarseTiles(n) tiles.
+template <typename T>
+int launchPackSym(cudaStream_t s, const T* K, int64_t n, T* tiles);
 
 // CG vector updates on flat arrays of length n.
 // x += alpha p ; r -= alpha Ap ; rr -> EPI_CONV
