@@ -246,3 +246,19 @@ def test_setup_rejects_bad_input_with_status_codes():
     assert create(np.zeros_like(vox)) == 7
     assert create(vox, fx=np.array([10 ** 6], np.int64)) == 1
     assert create(vox) == 0
+
+
+def test_rhs_checks_and_host_transfers(case):
+    """A non-finite right-hand side is rejected on the device (status 1) and the
+    problem stays usable; the solution returned through the host arrays equals
+    the device-resident solve's."""
+    A, f = case["A"], case["f"]
+    bad = f.copy()
+    bad[len(bad) // 2] = np.nan
+    with pytest.raises(api.VfemError) as ei:
+        A.set_rhs(bad)
+    assert ei.value.status == 1
+    u, st = A.solve(f, precision="mixed")
+    A.set_rhs(f)
+    ud, std = A.solve_device(want_solution=True, precision="mixed")
+    assert np.array_equal(u, ud) and st["iterations"] == std["iterations"]

@@ -20,6 +20,7 @@
 #include <map>
 #include <string>
 #include <tuple>
+#include <thread>
 #include <type_traits>
 #include <vector>
 
@@ -100,7 +101,9 @@ struct vfem_problem {
     Scalars* S = nullptr;
     Scalars* hS = nullptr;
     RedBuf rb{};
-    // compressed staging
+    // compressed staging (measured on GB300: kernels reading and writing the
+    // caller's pageable host arrays directly were slower than these copies)
+    unsigned* dFlag = nullptr;  // non-finite input flag of the scatter
     double* dComp = nullptr;  // 3 * nused(level 0) (largest level)
     double* hIn = nullptr;    // pinned
     double* hOut = nullptr;   // pinned
@@ -157,6 +160,7 @@ void freeProblem(vfem_problem* p) {
     cudaFree(p->x32);
     cudaFree(p->freeDof); cudaFree(p->Kinv64); cudaFree(p->Kinv32); cudaFree(p->cb64); cudaFree(p->cb32);
     cudaFree(p->KinvV64); cudaFree(p->KinvV32); cudaFree(p->dFreeNode); cudaFree(p->cpart);
+    cudaFree(p->dFlag);
     cudaFree(p->S); cudaFree(p->rb.partials); cudaFree(p->rb.ticket); cudaFree(p->dComp);
     if (p->hS) cudaFreeHost(p->hS);
     if (p->hIn) cudaFreeHost(p->hIn);
@@ -526,6 +530,7 @@ vfem_status createImpl(const uint8_t* vox, int nx, int ny, int nz, const double*
     CKP(dalloc(&p->rb.partials, 2 * (int64_t)kMaxRedBlocks));
     CKP(dalloc(&p->rb.ticket, 1));
     CKP(dalloc(&p->dComp, 3 * p->L[0].nused));
+    CKP(dalloc(&p->dFlag, 1));
     CKP(cudaMallocHost((void**)&p->hS, sizeof(Scalars)));
     CKP(cudaMallocHost((void**)&p->hIn, sizeof(double) * 3 * (size_t)std::max<int64_t>(1, p->L[0].nused)));
     CKP(cudaMallocHost((void**)&p->hOut, sizeof(double) * 3 * (size_t)std::max<int64_t>(1, p->L[0].nused)));
@@ -879,14 +884,41 @@ vfem_status solveImpl(vfem_problem* p, const vfem_options* optIn, bool haveX0, v
     return result;
 }
 
-vfem_status toDenseHost(vfem_problem* p, int lv, const double* host, double* dense, double* h2dMs) {
+// Host compressed vector -> dense device vector of level lv.  checkFinite: the
+// scatter flags non-finite input (read back by the caller after a sync).
+// memcpy split over host threads for large host <-> pinned copies (one thread
+// copies ~10 GB/s on the Grace host; the staging copies are 8 bytes per DOF).
+void hostCopy(void* dst, const void* src, size_t bytes) {
+    const size_t kSlice = (size_t)32 << 20;
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const size_t nt = std::min<size_t>({(size_t)8, (size_t)hw, (bytes + kSlice - 1) / kSlice});
+    if (nt <= 1) {
+        std::memcpy(dst, src, bytes);
+        return;
+    }
+    const size_t chunk = (bytes / nt + 63) & ~(size_t)63;
+    std::vector<std::thread> th;
+    for (size_t t = 1; t < nt; ++t) {
+        const size_t off = t * chunk;
+        if (off >= bytes) break;
+        const size_t len = std::min(chunk, bytes - off);
+        th.emplace_back([=] { std::memcpy((char*)dst + off, (const char*)src + off, len); });
+    }
+    std::memcpy(dst, src, std::min(chunk, bytes));
+    for (auto& t : th) t.join();
+}
+
+// Host compressed vector -> dense device vector of level lv.  checkFinite: the
+// scatter flags non-finite input (read back by the caller after a sync).
+vfem_status toDenseHost(vfem_problem* p, int lv, const double* host, double* dense, bool checkFinite) {
     DevLevel& l = p->L[lv];
-    std::memcpy(p->hIn, host, sizeof(double) * 3 * (size_t)l.nused);
+    hostCopy(p->hIn, host, sizeof(double) * 3 * (size_t)l.nused);
     CK(cudaMemcpyAsync(p->dComp, p->hIn, sizeof(double) * 3 * (size_t)l.nused, cudaMemcpyHostToDevice, p->stream));
     CK(cudaMemsetAsync(dense, 0, sizeof(double) * (size_t)l.nvec(), p->stream));
-    p->launches += launchScatterCompressed<double>(p->stream, l.nused, l.nodeStore, p->dComp, dense);
+    if (checkFinite) CK(cudaMemsetAsync(p->dFlag, 0, sizeof(unsigned), p->stream));
+    p->launches += launchScatterCompressed<double>(p->stream, l.nused, l.nodeStore, p->dComp, dense,
+                                                   checkFinite ? p->dFlag : nullptr);
     g_launches += 1;
-    (void)h2dMs;
     return VFEM_OK;
 }
 
@@ -896,7 +928,7 @@ vfem_status fromDenseHost(vfem_problem* p, int lv, const double* dense, double* 
     g_launches += 1;
     CK(cudaMemcpyAsync(p->hOut, p->dComp, sizeof(double) * 3 * (size_t)l.nused, cudaMemcpyDeviceToHost, p->stream));
     CK(cudaStreamSynchronize(p->stream));
-    std::memcpy(host, p->hOut, sizeof(double) * 3 * (size_t)l.nused);
+    hostCopy(host, p->hOut, sizeof(double) * 3 * (size_t)l.nused);
     return VFEM_OK;
 }
 
@@ -972,11 +1004,13 @@ vfem_status vfem_problem_info(const vfem_problem* p, int32_t level, int64_t* num
 vfem_status vfem_problem_set_rhs(vfem_problem* p, const double* f) {
     if (!p || !f) return fail(VFEM_ERR_INVALID_ARGUMENT, "null argument");
     CK(cudaSetDevice(p->device));
-    for (int64_t i = 0; i < 3 * p->L[0].nused; ++i)
-        if (!std::isfinite(f[i])) return fail(VFEM_ERR_INVALID_ARGUMENT, "non-finite right-hand side");
-    vfem_status s = toDenseHost(p, 0, f, p->f64, nullptr);
+    p->rhsSet = false;
+    vfem_status s = toDenseHost(p, 0, f, p->f64, true);
     if (s != VFEM_OK) return s;
+    unsigned bad = 0;
+    CK(cudaMemcpyAsync(&bad, p->dFlag, sizeof(unsigned), cudaMemcpyDeviceToHost, p->stream));
     CK(cudaStreamSynchronize(p->stream));
+    if (bad) return fail(VFEM_ERR_INVALID_ARGUMENT, "non-finite right-hand side");
     p->rhsSet = true;
     return VFEM_OK;
 }
@@ -1010,7 +1044,7 @@ vfem_status vfem_solve(vfem_problem* p, const vfem_options* opt, const double* u
     CK(cudaSetDevice(p->device));
     if (st) std::memset(st, 0, sizeof(*st));
     if (u0) {
-        vfem_status s0 = toDenseHost(p, 0, u0, p->x64, nullptr);
+        vfem_status s0 = toDenseHost(p, 0, u0, p->x64, false);
         if (s0 != VFEM_OK) return s0;
     }
     vfem_status s = solveImpl(p, opt, u0 != nullptr, st);
@@ -1024,7 +1058,7 @@ vfem_status vfem_solve(vfem_problem* p, const vfem_options* opt, const double* u
 vfem_status vfem_apply_operator(vfem_problem* p, const double* x, double* y) {
     if (!p || !x || !y) return fail(VFEM_ERR_INVALID_ARGUMENT, "null argument");
     CK(cudaSetDevice(p->device));
-    vfem_status s = toDenseHost(p, 0, x, p->p64, nullptr);
+    vfem_status s = toDenseHost(p, 0, x, p->p64, false);
     if (s != VFEM_OK) return s;
     MatvecArgs<double> a = mvArgs<double>(p, 0, p->p64, p->Ap64, MV_AX);
     a.checkDone = 0;
@@ -1056,7 +1090,7 @@ vfem_status vfem_apply_preconditioner(vfem_problem* p, int32_t mg_mode, const do
     DevLevel& l0 = p->L[0];
     vfem_status s = ensureCoarse<double>(p, mg_mode == VFEM_MG_VCYCLE);
     if (s != VFEM_OK) return s;
-    s = toDenseHost(p, 0, r, l0.r64, nullptr);
+    s = toDenseHost(p, 0, r, l0.r64, false);
     if (s != VFEM_OK) return s;
     vfem_options o;
     vfem_options_default(&o);
@@ -1076,7 +1110,7 @@ vfem_status vfem_restrict(vfem_problem* p, int32_t level, const double* fine, do
     CK(cudaSetDevice(p->device));
     DevLevel& lf = p->L[level];
     DevLevel& lc = p->L[level + 1];
-    vfem_status s = toDenseHost(p, level, fine, lf.t64, nullptr);
+    vfem_status s = toDenseHost(p, level, fine, lf.t64, false);
     if (s != VFEM_OK) return s;
     launchInitScalars(p->stream, p->S, 1e-6, 1, 0, 0, 0, 0.0);
     int k = 1 + launchRestrict<double>(ctx(p), lf.g, lc.g, lc.div, lf.t64, lc.t64, 0);
@@ -1092,7 +1126,7 @@ vfem_status vfem_interpolate(vfem_problem* p, int32_t level, const double* coars
     CK(cudaSetDevice(p->device));
     DevLevel& lf = p->L[level];
     DevLevel& lc = p->L[level + 1];
-    vfem_status s = toDenseHost(p, level + 1, coarse, lc.t64, nullptr);
+    vfem_status s = toDenseHost(p, level + 1, coarse, lc.t64, false);
     if (s != VFEM_OK) return s;
     launchInitScalars(p->stream, p->S, 1e-6, 1, 0, 0, 0, 0.0);
     CK(cudaMemsetAsync(lf.t64, 0, sizeof(double) * (size_t)lf.nvec(), p->stream));

@@ -1370,9 +1370,14 @@ __global__ void kFill(int64_t n, T* __restrict__ y, T v) {
 
 template <typename T>
 __global__ void kScatterCompressed(int64_t nn, const int32_t* __restrict__ store, const double* __restrict__ comp,
-                                   T* __restrict__ dense) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < 3 * nn; i += (int64_t)gridDim.x * blockDim.x)
-        dense[3 * (int64_t)store[i / 3] + i % 3] = (T)comp[i];
+                                   T* __restrict__ dense, unsigned* bad) {
+    bool ok = true;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < 3 * nn; i += (int64_t)gridDim.x * blockDim.x) {
+        const double v = comp[i];
+        ok = ok && isfinite(v);
+        dense[3 * (int64_t)store[i / 3] + i % 3] = (T)v;
+    }
+    if (bad && !ok) atomicOr(bad, 1u);
 }
 
 template <typename T>
@@ -1604,8 +1609,9 @@ int launchFill(cudaStream_t s, int64_t n, T* y, T v) {
 }
 
 template <typename T>
-int launchScatterCompressed(cudaStream_t s, int64_t nn, const int32_t* store, const double* comp, T* dense) {
-    kScatterCompressed<T><<<flatBlocks(3 * nn), NT, 0, s>>>(nn, store, comp, dense);
+int launchScatterCompressed(cudaStream_t s, int64_t nn, const int32_t* store, const double* comp, T* dense,
+                            unsigned* bad) {
+    kScatterCompressed<T><<<flatBlocks(3 * nn), NT, 0, s>>>(nn, store, comp, dense, bad);
     return 1;
 }
 
@@ -1729,7 +1735,7 @@ cudaError_t launchMatvecNoAlloc(cudaStream_t s, const MatvecArgs<double>& a, boo
     template int launchUpdateP<T>(const LaunchCtx&, int64_t, T*, const T*, int);                                     \
     template int launchDots<T>(const LaunchCtx&, int64_t, const T*, const T*, const T*, const T*, int, int);         \
     template int launchFill<T>(cudaStream_t, int64_t, T*, T);                                                        \
-    template int launchScatterCompressed<T>(cudaStream_t, int64_t, const int32_t*, const double*, T*);               \
+    template int launchScatterCompressed<T>(cudaStream_t, int64_t, const int32_t*, const double*, T*, unsigned*);    \
     template int launchGatherCompressed<T>(cudaStream_t, int64_t, const int32_t*, const T*, double*);               \
     template int launchAssembleCoarse<T>(cudaStream_t, const Grid&, const float*, const int32_t*, const double*,     \
                                          double, T*, int64_t);                                                       \

@@ -153,7 +153,10 @@ int launchFill(cudaStream_t s, int64_t n, T* y, T v);
 
 // compressed <-> dense storage
 template <typename T>
-int launchScatterCompressed(cudaStream_t s, int64_t nnodes, const int32_t* nodeStore, const double* comp, T* dense);
+// comp may be host memory when the device reads pageable memory directly; bad
+// (optional) gets bit 0 set when comp holds a non-finite value.
+int launchScatterCompressed(cudaStream_t s, int64_t nnodes, const int32_t* nodeStore, const double* comp, T* dense,
+                            unsigned* bad = nullptr);
 template <typename T>
 int launchGatherCompressed(cudaStream_t s, int64_t nnodes, const int32_t* nodeStore, const T* dense, double* comp);
 
