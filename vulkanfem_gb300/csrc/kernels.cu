@@ -266,28 +266,6 @@ struct Kd {
     T v[576];
 };
 
-// In-place 8-point Walsh-Hadamard transform of each displacement component:
-// v[3m+c] = sum_a (-1)^popcount(m&a) u[3a+c].
-template <typename T>
-__device__ __forceinline__ void fwht8x3(T (&v)[24]) {
-#pragma unroll
-    for (int s = 1; s < 8; s <<= 1) {
-#pragma unroll
-        for (int a = 0; a < 8; ++a) {
-            if (a & s) continue;
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                T p = v[3 * a + c], q = v[3 * (a + s) + c];
-                v[3 * a + c] = p + q;
-                v[3 * (a + s) + c] = p - q;
-            }
-        }
-    }
-}
-
-// y = e * Ke u for an isotropic cube element: Ke = H^T Khat H with Khat on the
-// 45-entry pattern (8 symmetry classes), H the per-component Walsh-Hadamard
-// transform.  ~190 flops instead of 1152 for the dense 24x24 product.
 // y = Khat u on the 45-entry pattern (modes 1..7; mode 0, the rigid translation,
 // has no energy).  u and y hold 3 m + c for mode m and component c.
 template <typename T>
@@ -308,15 +286,6 @@ __device__ __forceinline__ void applyKhat(const T (&u)[24], T (&y)[24], const Ks
 #undef KS_
 }
 
-template <typename T>
-__device__ __forceinline__ void elemStruct(T (&u)[24], T (&y)[24], const Ks<T>& k, T e) {
-    fwht8x3(u);
-#pragma unroll
-    for (int i = 3; i < 24; ++i) u[i] *= e;
-    applyKhat<T>(u, y, k);
-    fwht8x3(y);
-}
-
 // y = e * Ke u, general symmetric Ke.
 template <typename T>
 __device__ __forceinline__ void elemDense(const T (&u)[24], T (&y)[24], const Kd<T>& k, T e) {
@@ -328,17 +297,6 @@ __device__ __forceinline__ void elemDense(const T (&u)[24], T (&y)[24], const Kd
         y[r] = s * e;
     }
 }
-
-template <typename T, bool STRUCT>
-struct KP;
-template <typename T>
-struct KP<T, true> {
-    typedef Ks<T> type;
-};
-template <typename T>
-struct KP<T, false> {
-    typedef Kd<T> type;
-};
 
 // Shared-memory node slots are padded to 4 values (x, y, z, unused) so that a
 // node moves with one 16-byte (float) or two 16-byte (double) accesses.
@@ -414,7 +372,10 @@ __device__ __forceinline__ void mvOutput(const MatvecArgs<T>& a, int64_t s, cons
     }
 }
 
-// Element-by-element product on a 2.5-D tile.  A block of 32 x 8 threads marches
+// Element-by-element product with a general (dense 24 x 24) Ke, for element
+// matrices without the isotropic-cube symmetry (for example the reference's
+// Ke0.dat in its own node order); structured Ke use kMatvecH below.
+// A 2.5-D tile: a block of 32 x 8 threads marches
 // up a z-range; at each element layer thread (tx,ty) computes the element whose
 // lower corner is node (x0+tx-1, y0+ty-1) and owns node (x0+tx, y0+ty), which is
 // the (1,1) corner of its own element and a corner of the three neighbouring
@@ -429,9 +390,9 @@ __device__ __forceinline__ void mvOutput(const MatvecArgs<T>& a, int64_t s, cons
 //
 // T is the storage type of the vectors, TC the arithmetic type (T, or df for
 // the true residual of the mixed-precision solve: FP64 vectors, df arithmetic).
-template <typename T, bool STRUCT, typename TC = T>
-__global__ void __launch_bounds__(MV_TX* MV_TY, STRUCT ? (sizeof(TC) == 4 ? 4 : 2) : 1)
-    kMatvec(MatvecArgs<T> a, const typename KP<TC, STRUCT>::type kp, Scalars* S, RedBuf rb) {
+template <typename T, typename TC = T>
+__global__ void __launch_bounds__(MV_TX* MV_TY, 1)
+    kMatvec(MatvecArgs<T> a, const Kd<TC> kp, Scalars* S, RedBuf rb) {
     if (a.checkDone && S->done) return;
     if (a.condTrue && !trueResidualDue(S)) return;
     typedef Cvt<T, TC> C;
@@ -517,8 +478,7 @@ __global__ void __launch_bounds__(MV_TX* MV_TY, STRUCT ? (sizeof(TC) == 4 ? 4 : 
                 const int dx = n & 1, dy = (n >> 1) & 1, dz = n >> 2;
                 ldSlot<TC>(SU((k + dz) & 1, ty + dy, tx + dx), u[3 * n], u[3 * n + 1], u[3 * n + 2]);
             }
-            if constexpr (STRUCT) elemStruct<TC>(u, ye, kp, sc * TC(Ee));
-            else elemDense<TC>(u, ye, kp, sc * TC(Ee));
+            elemDense<TC>(u, ye, kp, sc * TC(Ee));
         } else {
 #pragma unroll
             for (int i = 0; i < 24; ++i) ye[i] = TC(0);
@@ -1456,9 +1416,9 @@ cudaError_t setKernelAttributes() {
     if ((e = cudaFuncSetAttribute(kMatvecH<double, double, OUT_CG>, A, s64))) return e;
     if ((e = cudaFuncSetAttribute(kMatvecH<double, df, OUT_TRUE>, A, sdf))) return e;
     if ((e = cudaFuncSetAttribute(kMatvecH<double, df>, A, sdf))) return e;
-    if ((e = cudaFuncSetAttribute(kMatvec<double, false>, A, s64))) return e;
-    if ((e = cudaFuncSetAttribute(kMatvec<float, false>, A, s32))) return e;
-    return cudaFuncSetAttribute(kMatvec<double, false, df>, A, sdf);
+    if ((e = cudaFuncSetAttribute(kMatvec<double>, A, s64))) return e;
+    if ((e = cudaFuncSetAttribute(kMatvec<float>, A, s32))) return e;
+    return cudaFuncSetAttribute(kMatvec<double, df>, A, sdf);
 }
 
 template <typename T>
@@ -1479,7 +1439,7 @@ int launchMatvec(const LaunchCtx& c, const MatvecArgs<T>& a, bool structured, co
         Kd<T> k;
         const T* src = static_cast<const T*>(opconst) + 45;
         for (int i = 0; i < 576; ++i) k.v[i] = src[i];
-        kMatvec<T, false><<<grid, block, smem, c.stream>>>(a, k, c.S, c.rb);
+        kMatvec<T><<<grid, block, smem, c.stream>>>(a, k, c.S, c.rb);
     }
     return 1;
 }
@@ -1499,7 +1459,7 @@ int launchMatvecDF(const LaunchCtx& c, const MatvecArgs<double>& a, bool structu
     } else {
         Kd<df> k;
         for (int i = 0; i < 576; ++i) k.v[i] = df(opconst[45 + i]);
-        kMatvec<double, false, df><<<grid, block, smem, c.stream>>>(a, k, c.S, c.rb);
+        kMatvec<double, df><<<grid, block, smem, c.stream>>>(a, k, c.S, c.rb);
     }
     return 1;
 }
@@ -1713,7 +1673,7 @@ cudaError_t launchMatvecNoAlloc(cudaStream_t s, const MatvecArgs<double>& a, boo
     } else {
         Kd<double> k;
         for (int i = 0; i < 576; ++i) k.v[i] = static_cast<const double*>(opconst)[45 + i];
-        kMatvec<double, false><<<grid, block, smem, s>>>(b, k, S, rb);
+        kMatvec<double><<<grid, block, smem, s>>>(b, k, S, rb);
     }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     return cudaMemcpyAsync(xKx, &S->red0, sizeof(double), cudaMemcpyDeviceToDevice, s);
