@@ -86,13 +86,15 @@ struct vfem_problem {
     int64_t nc = 0;
     int32_t* freeDof = nullptr;
     // Coarsest dense inverses, built on first use (ensureCoarse): FP64 (full
-    // n x n) for the FP64 solver and preconditioner, FP32 (the packed lower block
-    // triangle of 64 x 64 tiles, launchPackSym) for the mixed one; V = the
-    // multiplicative cycle's operator (volume-averaged modulus).
+    // n x n) for the FP64 solver and preconditioner; for the mixed one the FP32
+    // inverse packed as the lower block triangle of 64 x 64 FP16 tiles
+    // (launchPackSymHalf) with its power-of-two scale; V = the multiplicative
+    // cycle's operator (volume-averaged modulus).
     double* Kinv64 = nullptr;
-    float* Kinv32 = nullptr;
     double* KinvV64 = nullptr;
-    float* KinvV32 = nullptr;
+    __half* KinvH = nullptr;
+    __half* KinvVH = nullptr;
+    float scaleH = 1.0f, scaleVH = 1.0f;
     int32_t* dFreeNode = nullptr;  // coarsest storage node -> free node id (assembly)
     double* cb64 = nullptr;        // gathered coarse right-hand side, coarseBlocks(nc) * 64 (zero tail)
     float* cb32 = nullptr;
@@ -158,8 +160,8 @@ void freeProblem(vfem_problem* p) {
     }
     cudaFree(p->f64); cudaFree(p->x64); cudaFree(p->p64); cudaFree(p->Ap64); cudaFree(p->p32); cudaFree(p->Ap32);
     cudaFree(p->x32);
-    cudaFree(p->freeDof); cudaFree(p->Kinv64); cudaFree(p->Kinv32); cudaFree(p->cb64); cudaFree(p->cb32);
-    cudaFree(p->KinvV64); cudaFree(p->KinvV32); cudaFree(p->dFreeNode); cudaFree(p->cpart);
+    cudaFree(p->freeDof); cudaFree(p->Kinv64); cudaFree(p->KinvH); cudaFree(p->cb64); cudaFree(p->cb32);
+    cudaFree(p->KinvV64); cudaFree(p->KinvVH); cudaFree(p->dFreeNode); cudaFree(p->cpart);
     cudaFree(p->dFlag);
     cudaFree(p->S); cudaFree(p->rb.partials); cudaFree(p->rb.ticket); cudaFree(p->dComp);
     if (p->hS) cudaFreeHost(p->hS);
@@ -305,44 +307,69 @@ vfem_status invertCoarse(vfem_problem* p, const float* E, double scale, T* K) {
 }
 
 template <typename T>
-T*& kinvSlot(vfem_problem* p, bool v);
-template <>
-double*& kinvSlot<double>(vfem_problem* p, bool v) { return v ? p->KinvV64 : p->Kinv64; }
-template <>
-float*& kinvSlot<float>(vfem_problem* p, bool v) { return v ? p->KinvV32 : p->Kinv32; }
+vfem_status ensureCoarse(vfem_problem* p, bool vcycle);
 
-// Build the coarsest inverse a solve or preconditioner of this type and cycle
-// needs (once).  An FP32 factorisation that fails (a system too ill-conditioned
-// for FP32) falls back to the FP64 inverse rounded to FP32.
-template <typename T>
-vfem_status ensureCoarse(vfem_problem* p, bool vcycle) {
+// FP64: the full matrix, applied by a one-FMA-per-value GEMV.
+template <>
+vfem_status ensureCoarse<double>(vfem_problem* p, bool vcycle) {
     if (p->nc == 0) return VFEM_OK;
-    T*& K = kinvSlot<T>(p, vcycle);
+    double*& K = vcycle ? p->KinvV64 : p->Kinv64;
     if (K) return VFEM_OK;
-    // FP64: the full matrix (applied by a one-FMA-per-value GEMV); FP32: packed tiles.
-    const bool packedForm = std::is_same<T, float>::value;
-    const int64_t n = p->nc, stored = packedForm ? coarseTiles(n) * CT * CT : n * n;
-    T* out = nullptr;
-    CK(dalloc(&out, stored));
-    T* full = out;
-    if (packedForm && dalloc(&full, n * n) != cudaSuccess) {
+    double* out = nullptr;
+    CK(dalloc(&out, p->nc * p->nc));
+    const DevLevel& dc = p->L.back();
+    const vfem_status st = invertCoarse<double>(p, vcycle ? dc.Ev : dc.E, dc.scale, out);
+    if (st != VFEM_OK) {
+        cudaFree(out);
+        return st;
+    }
+    K = out;
+    return VFEM_OK;
+}
+
+// Mixed precision: factorised and inverted in FP32, stored as packed FP16
+// tiles scaled by a power of two (the rounding error of the FP16 values,
+// 2^-11 relative, is of the order of the FP32 inverse's own error for the
+// coarse systems' condition numbers).  An FP32 factorisation that fails (a
+// system too ill-conditioned for FP32) falls back to the FP64 inverse.
+template <>
+vfem_status ensureCoarse<float>(vfem_problem* p, bool vcycle) {
+    if (p->nc == 0) return VFEM_OK;
+    __half*& K = vcycle ? p->KinvVH : p->KinvH;
+    if (K) return VFEM_OK;
+    const int64_t n = p->nc;
+    __half* out = nullptr;
+    float* full = nullptr;
+    CK(dalloc(&out, coarseTiles(n) * CT * CT));
+    if (dalloc(&full, n * n + 1) != cudaSuccess) {
         cudaFree(out);
         return fail(VFEM_ERR_OUT_OF_MEMORY, "coarse inverse workspace");
     }
     const DevLevel& dc = p->L.back();
-    vfem_status st = invertCoarse<T>(p, vcycle ? dc.Ev : dc.E, dc.scale, full);
-    if (st == VFEM_OK && packedForm) {
-        p->launches += launchPackSym<T>(p->stream, full, n, out);
-        if (cudaStreamSynchronize(p->stream) != cudaSuccess) st = fail(VFEM_ERR_CUDA, "coarse inverse packing");
-    } else if (st == VFEM_ERR_SINGULAR && packedForm) {
+    vfem_status st = invertCoarse<float>(p, vcycle ? dc.Ev : dc.E, dc.scale, full);
+    if (st == VFEM_ERR_SINGULAR) {
         st = ensureCoarse<double>(p, vcycle);
-        if (st == VFEM_OK) {
-            launchConvert<double, T>(p->stream, n * n, kinvSlot<double>(p, vcycle), full);
-            p->launches += 1 + launchPackSym<T>(p->stream, full, n, out);
-            if (cudaStreamSynchronize(p->stream) != cudaSuccess) st = fail(VFEM_ERR_CUDA, "coarse inverse copy");
-        }
+        if (st == VFEM_OK) p->launches += launchConvert<double, float>(p->stream, n * n, vcycle ? p->KinvV64 : p->Kinv64, full);
     }
-    if (full != out) cudaFree(full);
+    float maxDiag = 0.0f;
+    if (st == VFEM_OK) {
+        p->launches += launchMaxDiag(p->stream, full, n, full + n * n);
+        if (cudaMemcpyAsync(&maxDiag, full + n * n, sizeof(float), cudaMemcpyDeviceToHost, p->stream) != cudaSuccess ||
+            cudaStreamSynchronize(p->stream) != cudaSuccess)
+            st = fail(VFEM_ERR_CUDA, "coarse inverse diagonal");
+        else if (!(maxDiag > 0.0f) || !std::isfinite(maxDiag))
+            st = fail(VFEM_ERR_SINGULAR, "coarsest inverse has no positive diagonal");
+    }
+    float& scale = vcycle ? p->scaleVH : p->scaleH;
+    if (st == VFEM_OK) {
+        // scale = 2^(e - 14) with maxDiag <= 2^e: stored diagonal in (2^13, 2^14].
+        int e = 0;
+        std::frexp(maxDiag, &e);
+        scale = std::ldexp(1.0f, e - 14);
+        p->launches += launchPackSymHalf(p->stream, full, n, 1.0f / scale, out);
+        if (cudaStreamSynchronize(p->stream) != cudaSuccess) st = fail(VFEM_ERR_CUDA, "coarse inverse packing");
+    }
+    cudaFree(full);
     if (st != VFEM_OK) {
         cudaFree(out);
         return st;
@@ -579,17 +606,13 @@ const void* opc<double>(vfem_problem* p) { return p->op64; }
 template <>
 const void* opc<float>(vfem_problem* p) { return p->op32; }
 template <typename T>
-T* kinv(vfem_problem* p);
+CoarseInv<T> kinv(vfem_problem* p, bool vcycle);
 template <>
-double* kinv<double>(vfem_problem* p) { return p->Kinv64; }
+CoarseInv<double> kinv<double>(vfem_problem* p, bool vcycle) { return {vcycle ? p->KinvV64 : p->Kinv64}; }
 template <>
-float* kinv<float>(vfem_problem* p) { return p->Kinv32; }
-template <typename T>
-T* kinvV(vfem_problem* p);
-template <>
-double* kinvV<double>(vfem_problem* p) { return p->KinvV64; }
-template <>
-float* kinvV<float>(vfem_problem* p) { return p->KinvV32; }
+CoarseInv<float> kinv<float>(vfem_problem* p, bool vcycle) {
+    return vcycle ? CoarseInv<float>{p->KinvVH, p->scaleVH} : CoarseInv<float>{p->KinvH, p->scaleH};
+}
 template <typename T>
 T* cbuf(vfem_problem* p);
 template <>
@@ -634,7 +657,7 @@ int vcycle(vfem_problem* p, const vfem_options& o, int lv, T* r, T* z, T** outZ,
     LaunchCtx c = ctx(p);
     if (lv == L - 1) {
         // Coarsest: exact dense-inverse solve on the free DOFs; fixed and unused DOFs stay 0.
-        n += launchCoarseSolve<T>(c, o.mg_mode == VFEM_MG_VCYCLE ? kinvV<T>(p) : kinv<T>(p), p->nc, p->freeDof, r,
+        n += launchCoarseSolve<T>(c, kinv<T>(p, o.mg_mode == VFEM_MG_VCYCLE), p->nc, p->freeDof, r,
                                   cbuf<T>(p), reinterpret_cast<T*>(p->cpart), z, 1);
         if (lv == 0 && epi != EPI_NONE) n += launchDots<T>(c, l.nvec(), r, z, aux ? z : nullptr, aux, epi, 1);
         *outZ = z;
@@ -1194,12 +1217,12 @@ vfem_status vfem_profile_kernels(vfem_problem* p, int32_t reps, double* ms) {
                     return launchUpdateP<float>(c, n, p->p32, l0.z32, 0);
                 case VFEM_K_COARSE_FP64: {
                     DevLevel& lc = p->L.back();
-                    return launchCoarseSolve<double>(c, p->Kinv64, p->nc, p->freeDof, lc.r64, p->cb64, p->cpart,
+                    return launchCoarseSolve<double>(c, kinv<double>(p, false), p->nc, p->freeDof, lc.r64, p->cb64, p->cpart,
                                                      lc.z64, 1);
                 }
                 case VFEM_K_COARSE_FP32: {
                     DevLevel& lc = p->L.back();
-                    return launchCoarseSolve<float>(c, p->Kinv32, p->nc, p->freeDof, lc.r32, p->cb32,
+                    return launchCoarseSolve<float>(c, kinv<float>(p, false), p->nc, p->freeDof, lc.r32, p->cb32,
                                                     reinterpret_cast<float*>(p->cpart), lc.z32, 1);
                 }
                 default: {

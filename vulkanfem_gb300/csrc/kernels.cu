@@ -1123,12 +1123,18 @@ __global__ void __launch_bounds__(256) kGemv64(const double* __restrict__ K, int
     if (lane == 0) zc[freeDof[row]] = acc;
 }
 
-// ---- coarsest solve: y = Kinv b with the symmetric inverse stored once.
-// Kinv is kept as the lower block triangle of 64 x 64 tiles (tile (I, J <= I) at
-// index I (I + 1) / 2 + J, row-major inside, zero-padded past n), half the bytes
-// of the full matrix.  kSymTile reads each tile once and writes its two partial
-// products, K_IJ b_J (for y_I) and K_IJ^T b_I (for y_J, off-diagonal tiles);
-// kSymReduce sums them per row block in a fixed order (deterministic, no atomics).
+// ---- coarsest solve of the mixed-precision cycle: y = Kinv b with the
+// symmetric inverse stored once, in FP16.  Kinv is kept as the lower block
+// triangle of 64 x 64 tiles (tile (I, J <= I) at index I (I + 1) / 2 + J,
+// row-major inside, zero-padded past n), a quarter of the bytes of the full
+// FP32 matrix.  The stored values are Kinv / scale with scale a power of two
+// that maps the largest diagonal entry to 2^14 (|Kinv_ij| <= max diag for an
+// SPD inverse), so every entry above 2^-10 of that maximum keeps FP16's 11-bit
+// significand; the products accumulate in FP32.  The rounding is symmetric, so
+// the coarse operator stays symmetric.  kSymTile reads each tile once and writes
+// its two partial products, K_IJ b_J (for y_I) and K_IJ^T b_I (for y_J,
+// off-diagonal tiles); kSymReduce sums them per row block in a fixed order
+// (deterministic, no atomics) and applies the scale.
 __host__ __device__ inline int64_t symTileCount(int64_t nb) { return nb * (nb + 1) / 2; }
 // Tile index -> (I, J): FP32 square root, corrected exactly in integers (an FP64
 // square root per thread would run on GB300's narrow FP64 pipe).
@@ -1140,25 +1146,42 @@ __device__ inline void symTileDecode(int64_t t, int64_t& I, int64_t& J) {
     J = t - i * (i + 1) / 2;
 }
 
-template <typename T>
-__global__ void kPackSym(const T* __restrict__ K, int64_t n, int64_t nb, T* __restrict__ tiles) {
+__global__ void kPackSymHalf(const float* __restrict__ K, int64_t n, int64_t nb, float invScale,
+                             __half* __restrict__ tiles) {
     const int64_t total = symTileCount(nb) * CT * CT;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
         int64_t I, J;
         symTileDecode(i / (CT * CT), I, J);
         const int e = (int)(i % (CT * CT));
         const int64_t row = I * CT + e / CT, col = J * CT + e % CT;
-        tiles[i] = (row < n && col < n) ? (T)K[row * n + col] : T(0);
+        tiles[i] = __float2half_rn((row < n && col < n) ? K[row * n + col] * invScale : 0.0f);
     }
 }
 
-// One tile per block: 16 x 16 threads, each a 4 x 4 sub-block (four 16-byte
+// Largest diagonal entry of a row-major n x n matrix (one block).
+__global__ void __launch_bounds__(1024) kMaxDiag(const float* __restrict__ K, int64_t n, float* __restrict__ out) {
+    __shared__ float red[32];
+    float m = 0.0f;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) m = fmaxf(m, K[i * n + i]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        m = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (threadIdx.x == 0) *out = m;
+    }
+}
+
+// One tile per block: 16 x 16 threads, each a 4 x 4 sub-block (four 8-byte
 // row loads).  Row sums reduce over the 16 column groups by shuffles; column
 // sums over the two row groups of a warp by one shuffle, then over the 8
 // warps in shared memory.  part holds 2 x 64 values per tile.
-template <typename T>
-__global__ void __launch_bounds__(256) kSymTile(const T* __restrict__ tiles, const T* __restrict__ b,
-                                                T* __restrict__ part, const Scalars* S, int checkDone) {
+__global__ void __launch_bounds__(256) kSymTile(const __half* __restrict__ tiles, const float* __restrict__ b,
+                                                float* __restrict__ part, const Scalars* S, int checkDone) {
+    typedef float T;
     if (checkDone && S->done) return;
     __shared__ T colp[8][CT];
     const int64_t t = blockIdx.x;
@@ -1166,7 +1189,7 @@ __global__ void __launch_bounds__(256) kSymTile(const T* __restrict__ tiles, con
     symTileDecode(t, I, J);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int tc = lane & 15, tr = warp * 2 + (lane >> 4);
-    const T* K = tiles + t * (CT * CT);
+    const __half* K = tiles + t * (CT * CT);
     T bJ[4], bI[4], rs[4], cs[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
@@ -1176,8 +1199,10 @@ __global__ void __launch_bounds__(256) kSymTile(const T* __restrict__ tiles, con
     }
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-        T k[4];
-        V4<T>::ld(K + (4 * tr + i) * CT + 4 * tc, k);
+        const uint2 raw = *reinterpret_cast<const uint2*>(K + (4 * tr + i) * CT + 4 * tc);
+        const float2 k01 = __half22float2(*reinterpret_cast<const __half2*>(&raw.x));
+        const float2 k23 = __half22float2(*reinterpret_cast<const __half2*>(&raw.y));
+        const T k[4] = {k01.x, k01.y, k23.x, k23.y};
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             rs[i] = fma(k[j], bJ[j], rs[i]);
@@ -1211,12 +1236,12 @@ __global__ void __launch_bounds__(256) kSymTile(const T* __restrict__ tiles, con
     }
 }
 
-// y_I = sum_{J <= I} (K_IJ b_J) + sum_{I' > I} (K_I'I^T b_I'); 16 groups of 64
-// threads split the tiles of row block I, then one group adds the 16 sums.
-template <typename T>
-__global__ void __launch_bounds__(1024) kSymReduce(const T* __restrict__ part, int64_t nb, int64_t n,
-                                                   const int32_t* __restrict__ freeDof, T* __restrict__ zc,
-                                                   const Scalars* S, int checkDone) {
+// y_I = scale (sum_{J <= I} (K_IJ b_J) + sum_{I' > I} (K_I'I^T b_I')); 16 groups
+// of 64 threads split the tiles of row block I, then one group adds the 16 sums.
+__global__ void __launch_bounds__(1024) kSymReduce(const float* __restrict__ part, int64_t nb, int64_t n,
+                                                   const int32_t* __restrict__ freeDof, float scale,
+                                                   float* __restrict__ zc, const Scalars* S, int checkDone) {
+    typedef float T;
     if (checkDone && S->done) return;
     __shared__ T red[16][CT];
     const int64_t I = blockIdx.x;
@@ -1231,7 +1256,7 @@ __global__ void __launch_bounds__(1024) kSymReduce(const T* __restrict__ part, i
 #pragma unroll
         for (int q = 0; q < 16; ++q) y += red[q][r];
         const int64_t i = I * CT + r;
-        if (i < n) zc[freeDof[i]] = y;
+        if (i < n) zc[freeDof[i]] = y * scale;
     }
 }
 
@@ -1511,25 +1536,29 @@ int launchProlongAdd(const LaunchCtx& c, const Grid& gf, const Grid& gc, int div
 }
 
 template <typename T>
-int launchCoarseSolve(const LaunchCtx& c, const T* Kinv, int64_t n, const int32_t* freeDof, const T* rc, T* tmp,
+int launchCoarseSolve(const LaunchCtx& c, CoarseInv<T> Kinv, int64_t n, const int32_t* freeDof, const T* rc, T* tmp,
                       T* part, T* zc, int checkDone) {
     if (n <= 0) return 0;
     kCoarseGather<T><<<(int)((n + 255) / 256), 256, 0, c.stream>>>(n, freeDof, rc, tmp, c.S, checkDone);
     if constexpr (std::is_same<T, double>::value) {
-        kGemv64<<<(int)((n * 32 + 255) / 256), 256, 0, c.stream>>>(Kinv, n, tmp, freeDof, zc, c.S, checkDone);
+        kGemv64<<<(int)((n * 32 + 255) / 256), 256, 0, c.stream>>>(Kinv.K, n, tmp, freeDof, zc, c.S, checkDone);
         return 2;
     } else {
         const int64_t nb = coarseBlocks(n);
-        kSymTile<T><<<(unsigned)symTileCount(nb), 256, 0, c.stream>>>(Kinv, tmp, part, c.S, checkDone);
-        kSymReduce<T><<<(unsigned)nb, 1024, 0, c.stream>>>(part, nb, n, freeDof, zc, c.S, checkDone);
+        kSymTile<<<(unsigned)symTileCount(nb), 256, 0, c.stream>>>(Kinv.K, tmp, part, c.S, checkDone);
+        kSymReduce<<<(unsigned)nb, 1024, 0, c.stream>>>(part, nb, n, freeDof, Kinv.scale, zc, c.S, checkDone);
         return 3;
     }
 }
 
-template <typename T>
-int launchPackSym(cudaStream_t s, const T* K, int64_t n, T* tiles) {
+int launchMaxDiag(cudaStream_t s, const float* K, int64_t n, float* out) {
+    kMaxDiag<<<1, 1024, 0, s>>>(K, n, out);
+    return 1;
+}
+
+int launchPackSymHalf(cudaStream_t s, const float* K, int64_t n, float invScale, __half* tiles) {
     const int64_t nb = coarseBlocks(n);
-    kPackSym<T><<<flatBlocks(symTileCount(nb) * CT * CT), NT, 0, s>>>(K, n, nb, tiles);
+    kPackSymHalf<<<flatBlocks(symTileCount(nb) * CT * CT), NT, 0, s>>>(K, n, nb, invScale, tiles);
     return 1;
 }
 
@@ -1689,9 +1718,8 @@ cudaError_t launchMatvecNoAlloc(cudaStream_t s, const MatvecArgs<double>& a, boo
                                      int);                                                                           \
     template int launchProlongAdd<T>(const LaunchCtx&, const Grid&, const Grid&, int, const T*, const uint8_t*, T*,  \
                                      int);                                                                           \
-    template int launchCoarseSolve<T>(const LaunchCtx&, const T*, int64_t, const int32_t*, const T*, T*, T*, T*,     \
-                                      int);                                                                          \
-    template int launchPackSym<T>(cudaStream_t, const T*, int64_t, T*);                                              \
+    template int launchCoarseSolve<T>(const LaunchCtx&, CoarseInv<T>, int64_t, const int32_t*, const T*, T*, T*,    \
+                                      T*, int);                                                                      \
     template int launchUpdateP<T>(const LaunchCtx&, int64_t, T*, const T*, int);                                     \
     template int launchDots<T>(const LaunchCtx&, int64_t, const T*, const T*, const T*, const T*, int, int);         \
     template int launchFill<T>(cudaStream_t, int64_t, T*, T);                                                        \

@@ -7,6 +7,7 @@
 // `done` once per chunk of iterations.
 #pragma once
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include "vfem_internal.h"
@@ -117,19 +118,33 @@ template <typename T>
 int launchProlongAdd(const LaunchCtx& c, const Grid& gf, const Grid& gc, int div, const T* zc,
                      const uint8_t* flags, T* zf, int checkDone);
 
-// Coarsest level: zc[free] = Kinv * rc[free].  FP32: Kinv is the packed lower
-// block triangle of CT x CT tiles (launchPackSym), tmp holds coarseBlocks(n) * CT
+// Coarsest level: zc[free] = Kinv * rc[free].  FP32 (the mixed-precision
+// cycle): Kinv is the packed lower block triangle of CT x CT tiles stored in
+// FP16 (launchPackSymHalf), value = scale * stored; tmp holds coarseBlocks(n) * CT
 // values (zero past n), part 2 * CT values per tile.  FP64: Kinv is the full
 // n x n matrix (part unused).
 constexpr int CT = 64;
 inline int64_t coarseBlocks(int64_t n) { return (n + CT - 1) / CT; }
 inline int64_t coarseTiles(int64_t n) { return coarseBlocks(n) * (coarseBlocks(n) + 1) / 2; }
 template <typename T>
-int launchCoarseSolve(const LaunchCtx& c, const T* Kinv, int64_t n, const int32_t* freeDof, const T* rc, T* tmp,
-                      T* part, T* zc, int checkDone);
-// Pack a full symmetric row-major n x n matrix into coarseTiles(n) tiles.
+struct CoarseInv;
+template <>
+struct CoarseInv<double> {
+    const double* K;
+};
+template <>
+struct CoarseInv<float> {
+    const __half* K;
+    float scale;
+};
 template <typename T>
-int launchPackSym(cudaStream_t s, const T* K, int64_t n, T* tiles);
+int launchCoarseSolve(const LaunchCtx& c, CoarseInv<T> Kinv, int64_t n, const int32_t* freeDof, const T* rc, T* tmp,
+                      T* part, T* zc, int checkDone);
+// *out = the largest diagonal entry of a row-major n x n matrix.
+int launchMaxDiag(cudaStream_t s, const float* K, int64_t n, float* out);
+// Pack a full symmetric row-major n x n matrix, times invScale, into
+// coarseTiles(n) FP16 tiles.
+int launchPackSymHalf(cudaStream_t s, const float* K, int64_t n, float invScale, __half* tiles);
 
 // CG vector updates on flat arrays of length n.
 // x += alpha p ; r -= alpha Ap ; rr -> EPI_CONV
