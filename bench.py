@@ -171,8 +171,9 @@ def algorithmic_bytes(kind, g0, g1, s):
     """Algorithmic bytes per launch on the finest level.  N = grid nodes, Ne = voxels
     (dense-grid model): matvec 6sN + Ne/8 + 4Ne + N/8 (x in, y out, occupancy bits,
     modulus, fixed bits); restrict 3sN_f + 3sN_c; prolong+smooth 3sN_c + 9sN_f (z_c,
-    r, D^-1 in; z out) + N_f/8; x/r update 18sN (x, r, p, Ap in; x, r out; the
-    mixed solve keeps its x correction in FP32 too); p update 9sN."""
+    r, D^-1 in; z out) + N_f/8; x/r update 18sN (x, r, p, Ap in; x, r out); p
+    update 9sN.  The mixed solve defers x += alpha p (its FP32 x correction) to
+    the p update: r update 9sN, p update 15sN (z, p, x in; p, x out)."""
     N, Ne = g0["nodes"], g0["voxels"]
     Nc = g1["nodes"]
     if kind == "matvec":
@@ -182,9 +183,9 @@ def algorithmic_bytes(kind, g0, g1, s):
     if kind == "prolong":
         return 3 * s * Nc + 9 * s * N + N / 8
     if kind == "update_xr":
-        return 18 * s * N
+        return (9 if s == 4 else 18) * s * N
     if kind == "update_p":
-        return 9 * s * N
+        return (15 if s == 4 else 9) * s * N
     raise KeyError(kind)
 
 

@@ -203,9 +203,9 @@ typedef enum vfem_kernel_class {
     VFEM_K_PROLONG_FP64 = 4,
     VFEM_K_PROLONG_FP32 = 5,
     VFEM_K_UPDATE_XR_FP64 = 6,
-    VFEM_K_UPDATE_XR_MIXED = 7,
+    VFEM_K_UPDATE_XR_MIXED = 7,   /* mixed: r -= alpha Ap and r.r (x += alpha p is deferred to the p update) */
     VFEM_K_UPDATE_P_FP64 = 8,
-    VFEM_K_UPDATE_P_FP32 = 9,
+    VFEM_K_UPDATE_P_FP32 = 9,     /* mixed: p = z + beta p with the deferred x += alpha p */
     VFEM_K_COARSE_FP64 = 10,
     VFEM_K_COARSE_FP32 = 11,
     VFEM_K_TRUE_RESIDUAL_DF = 12, /* f - K x on FP64 vectors in double-float arithmetic */

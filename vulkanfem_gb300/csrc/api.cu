@@ -754,8 +754,8 @@ int iteration(vfem_problem* p, const vfem_options& o, double** zOut64, float** z
         a.dot0 = DOT_X_OUT;
         a.epi = EPI_ALPHA;
         k += matvec<float>(p, a);
-        k += launchUpdateXR<float, float>(c, n, p->x32, l0.r32, p->p32, p->Ap32);
-        k += launchFlushX(c, n, p->x64, p->x32, 1);
+        k += launchUpdateR(c, n, l0.r32, p->Ap32);  // x += alpha p is deferred to launchUpdatePX / the flush
+        k += launchFlushX(c, n, p->x64, p->x32, p->p32, 1);
         // True residual f - K x64 in double-float; only its FP32 rounding (the new
         // recursive residual) and its norm are kept.
         MatvecArgs<double> t = mvArgs<double>(p, 0, p->x64, nullptr, MV_RESID);
@@ -767,7 +767,7 @@ int iteration(vfem_problem* p, const vfem_options& o, double** zOut64, float** z
         k += matvecDF(p, t);
         float* z = nullptr;
         k += precondition<float>(p, o, l0.r32, l0.z32, &z, o.flexible ? p->Ap32 : nullptr, EPI_BETA);
-        k += launchUpdateP<float>(c, n, p->p32, z, 0);
+        k += launchUpdatePX(c, n, p->p32, z, p->x32);
         *zOut32 = z;
     }
     return k;
@@ -861,7 +861,7 @@ vfem_status solveImpl(vfem_problem* p, const vfem_options* optIn, bool haveX0, v
         launches += cg.kernels;
         ++chunks;
     }
-    if (mixed) launches += launchFlushX(c, n, p->x64, p->x32, 0);  // fold any remaining FP32 correction
+    if (mixed) launches += launchFlushX(c, n, p->x64, p->x32, p->p32, 0);  // fold the remaining correction
     CK(cudaEventRecord(e1, p->stream));
     CK(cudaEventSynchronize(e1));
     float ms = 0;
@@ -1210,11 +1210,11 @@ vfem_status vfem_profile_kernels(vfem_problem* p, int32_t reps, double* ms) {
                 case VFEM_K_UPDATE_XR_FP64:
                     return launchUpdateXR<double, double>(c, n, p->x64, l0.r64, p->p64, p->Ap64);
                 case VFEM_K_UPDATE_XR_MIXED:
-                    return launchUpdateXR<float, float>(c, n, p->x32, l0.r32, p->p32, p->Ap32);
+                    return launchUpdateR(c, n, l0.r32, p->Ap32);
                 case VFEM_K_UPDATE_P_FP64:
                     return launchUpdateP<double>(c, n, p->p64, l0.z64, 0);
                 case VFEM_K_UPDATE_P_FP32:
-                    return launchUpdateP<float>(c, n, p->p32, l0.z32, 0);
+                    return launchUpdatePX(c, n, p->p32, l0.z32, p->x32);
                 case VFEM_K_COARSE_FP64: {
                     DevLevel& lc = p->L.back();
                     return launchCoarseSolve<double>(c, kinv<double>(p, false), p->nc, p->freeDof, lc.r64, p->cb64, p->cpart,

@@ -101,6 +101,7 @@ __device__ void applyEpi(int epi, Scalars* S, double t0, double t1) {
             break;
         case EPI_CONV:
             S->rr = t0;
+            S->rStamp = S->matvecs;
             if (!isfinite(t0)) S->done = BREAKDOWN;
             else if (t0 < S->threshold) {
                 if (S->mixed) S->checkPending = 1;
@@ -1105,6 +1106,168 @@ struct V4<double> {
     }
 };
 
+// The 2x up-leg in flat form (same values as kProlongSmooth2): a block owns
+// the fine rows [fy0, fy0 + PR) of fine layer fz, which are one contiguous
+// range of every fine vector, and a thread takes 4 consecutive nodes at a time
+// (12 values: three 16-byte loads of r and of dinv, three 16-byte stores of z,
+// one 4-byte load of the flags).  The coarse rows the block interpolates from
+// (PR/2 + 1 of them, averaged over the two coarse layers when fz is odd) are
+// copied to shared memory with asynchronous copies while the first chunk
+// loads, so a fine node costs 3-12 shared loads.  Only the first and last
+// chunk of a block, which the neighbouring blocks share, take the scalar path
+// (and every chunk when a vector is not 16-byte aligned).  Measured on GB300:
+// 16 rows per block beat 32 (a partial last wave of blocks) and a persistent
+// grid taking units from a counter (its per-unit barriers and counter round
+// trips cost more than the wave tail).
+constexpr int PR = 16;
+constexpr int kProlongCoarseRows = PR / 2 + 1;
+constexpr size_t kProlongFlatMaxSmem = 200 * 1024;
+__host__ __device__ inline int prolongFlatRowGroups(const Grid& gf) { return (gf.ny + PR - 1) / PR; }
+
+template <typename T>
+__device__ __forceinline__ void cpAsync(T* dst, const T* src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(d), "l"(src), "n"(sizeof(T)) : "memory");
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+    kProlongFlat(Grid gf, Grid gc, const T* __restrict__ zc, const T* __restrict__ rf, const T* __restrict__ dinv,
+                 const uint8_t* __restrict__ flags, T* __restrict__ zf, double coef, int maskFixed,
+                 const T* __restrict__ aux, int epi, int vec, float invNx, Scalars* S, RedBuf rb, int checkDone) {
+    if (checkDone && S->done) return;
+    extern __shared__ __align__(16) unsigned char prolongSmem[];
+    T* C = reinterpret_cast<T*>(prolongSmem);  // [kProlongCoarseRows][3 * gc.nx], then the layer above
+    const int groups = prolongFlatRowGroups(gf);
+    const int fz = blockIdx.x / groups;
+    const int fy0 = (blockIdx.x - fz * groups) * PR, fy1 = min(gf.ny, fy0 + PR);
+    const int cw = 3 * gc.nx, cy0 = fy0 >> 1, cz = fz >> 1;
+    const int nstage = min(kProlongCoarseRows, gc.ny - cy0) * cw;
+    const bool zodd = fz & 1;
+    const T half = T(0.5), cf = (T)coef;
+    {
+        // the block's coarse rows are contiguous in each coarse layer
+        const T* src = zc + 3 * gc.store(0, cy0, cz);
+        const int64_t up = 3 * ((int64_t)gc.nx * gc.ny);
+        for (int j = threadIdx.x; j < nstage; j += blockDim.x) {
+            cpAsync(C + j, src + j);
+            if (zodd) cpAsync(C + nstage + j, src + up + j);
+        }
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+    }
+    const int64_t nBeg = gf.store(0, fy0, fz);  // first node of the block
+    const int nb = (fy1 - fy0) * gf.nx;
+    const int64_t j1 = (nBeg + nb + 3) >> 2;
+    DotAcc<T> d0, d1;
+    // One chunk of 4 nodes; FULL: all 4 in the block's range and vectors aligned.
+    auto chunk = [&](auto fullTag, int64_t n0, int ln0, const T (&rv)[12], const T (&dv)[12], uint32_t fl4) {
+        constexpr bool FULL = decltype(fullTag)::value;
+        // (ly, fx) of the chunk's first node; fx < 0 for nodes before the range
+        const int lnc = max(ln0, 0);
+        int ly = __float2int_rz(((float)lnc + 0.5f) * invNx);
+        int fx = lnc - ly * gf.nx;
+        if (fx < 0) { --ly; fx += gf.nx; }
+        if (fx >= gf.nx) { ++ly; fx -= gf.nx; }
+        fx -= lnc - ln0;
+        T ov[12];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            const int ln = ln0 + t;
+            const bool in = FULL || (ln >= 0 && ln < nb);
+            if (in) {
+                const uint32_t fl = (fl4 >> (8 * t)) & 0xffu;
+                const bool used = (fl & FLAG_USED) != 0;
+                const bool zero = !used || (maskFixed && (fl & FLAG_FIXED));
+                const T* b = C + (ly >> 1) * cw + 3 * (fx >> 1);
+                T pv[3];
+                if (fx & 1) {
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) pv[c] = half * (b[c] + b[c + 3]);
+                } else {
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) pv[c] = b[c];
+                }
+                if (ly & 1) {
+                    const T* b1 = b + cw;
+                    if (fx & 1) {
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) pv[c] = half * (pv[c] + half * (b1[c] + b1[c + 3]));
+                    } else {
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) pv[c] = half * (pv[c] + b1[c]);
+                    }
+                }
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const T r = used ? rv[3 * t + c] : T(0);
+                    const T out = zero ? T(0) : pv[c] + cf * dv[3 * t + c] * r;
+                    if (epi != EPI_NONE) {
+                        d0.add(r * out);
+                        if (aux) d1.add(out * aux[3 * (n0 + t) + c]);
+                    }
+                    if (FULL) ov[3 * t + c] = out;
+                    else zf[3 * (n0 + t) + c] = out;
+                }
+            }
+            if (++fx == gf.nx) {
+                fx = 0;
+                ++ly;
+            }
+        }
+        if (FULL) {
+#pragma unroll
+            for (int v = 0; v < 3; ++v) V4<T>::st(zf + 3 * n0 + 4 * v, *reinterpret_cast<T(*)[4]>(ov + 4 * v));
+        }
+    };
+    bool staged = false;
+    for (int64_t j = (nBeg >> 2) + threadIdx.x;; j += blockDim.x) {
+        const bool have = j < j1;
+        const int64_t n0 = 4 * j;
+        const int ln0 = (int)(n0 - nBeg);  // -3 .. nb - 1
+        const bool full = vec && ln0 >= 0 && ln0 + 4 <= nb;
+        T rv[12], dv[12];
+        uint32_t fl4 = 0;
+        if (have) {
+            if (full) {
+#pragma unroll
+                for (int v = 0; v < 3; ++v) {
+                    V4<T>::ld(rf + 3 * n0 + 4 * v, *reinterpret_cast<T(*)[4]>(rv + 4 * v));
+                    V4<T>::ld(dinv + 3 * n0 + 4 * v, *reinterpret_cast<T(*)[4]>(dv + 4 * v));
+                }
+                fl4 = *reinterpret_cast<const uint32_t*>(flags + n0);
+            } else {
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    const bool in = ln0 + t >= 0 && ln0 + t < nb;
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        rv[3 * t + c] = in ? rf[3 * (n0 + t) + c] : T(0);
+                        dv[3 * t + c] = in ? dinv[3 * (n0 + t) + c] : T(0);
+                    }
+                    if (in) fl4 |= (uint32_t)flags[n0 + t] << (8 * t);
+                }
+            }
+        }
+        if (!staged) {
+            // every thread passes here once, after issuing its first chunk's loads
+            asm volatile("cp.async.wait_all;\n" ::: "memory");
+            __syncthreads();
+            if (zodd) {
+                for (int q = threadIdx.x; q < nstage; q += blockDim.x) C[q] = half * (C[q] + C[nstage + q]);
+                __syncthreads();
+            }
+            staged = true;
+        }
+        if (!have) break;
+        if (full) chunk(std::true_type{}, n0, ln0, rv, dv, fl4);
+        else chunk(std::false_type{}, n0, ln0, rv, dv, fl4);
+    }
+    if (epi != EPI_NONE) {
+        double v[2] = {d0.get(), d1.get()}, t[2];
+        if (gridReduce<256, 2>(v, rb, t)) applyEpi(epi, S, t[0], t[1]);
+    }
+}
+
 // y = Kinv b with the full inverse, one warp per row (FP64: the packed form below
 // needs two FMAs per stored value plus FP64 shuffle reductions, which GB300's
 // narrow FP64 pipe turns into 1.7x the time of this one-FMA-per-value form).
@@ -1298,14 +1461,80 @@ __global__ void __launch_bounds__(256) kUpdateXR(int64_t n, TX* __restrict__ x, 
     if (gridReduce<NT, 1>(v, rb, t)) applyEpi(EPI_CONV, S, t[0], 0.0);
 }
 
-// Mixed precision: fold the FP32 solution correction into the FP64 solution.
-// conditional = 1: only when an FP64 true-residual pass follows in this iteration.
+// Mixed precision: r -= alpha Ap; r.r.  The solution update x += alpha p of
+// the same iteration is deferred to kUpdatePX (or kFlushX), which read p anyway.
+__global__ void __launch_bounds__(256) kUpdateR(int64_t n, float* __restrict__ r, const float* __restrict__ Ap,
+                                                Scalars* S, RedBuf rb) {
+    if (S->done) return;
+    const float av = (float)S->alpha;
+    DotAcc<float> acc;
+    const int64_t tid = blockIdx.x * (int64_t)NT + threadIdx.x, stride = (int64_t)gridDim.x * NT;
+    const int64_t n4 = n / 4;
+    for (int64_t q = tid; q < n4; q += stride) {
+        float rv[4], av4[4];
+        V4<float>::ld(r + 4 * q, rv);
+        V4<float>::ld(Ap + 4 * q, av4);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            rv[k] = fma(-av, av4[k], rv[k]);
+            acc.add(rv[k] * rv[k]);
+        }
+        V4<float>::st(r + 4 * q, rv);
+    }
+    for (int64_t i = 4 * n4 + tid; i < n; i += stride) {
+        const float ri = fma(-av, Ap[i], r[i]);
+        r[i] = ri;
+        acc.add(ri * ri);
+    }
+    double v[1] = {acc.get()}, t[1];
+    if (gridReduce<NT, 1>(v, rb, t)) applyEpi(EPI_CONV, S, t[0], 0.0);
+}
+
+// Mixed precision: fold the FP32 solution correction, and this iteration's
+// deferred alpha p, into the FP64 solution.  conditional = 1: only when an FP64
+// true-residual pass follows in this iteration (kUpdateR has run, so alpha p is
+// pending; the stamp tells kUpdatePX it is folded).  conditional = 0 (after the
+// last iteration): alpha p only if kUpdateR ran in the last iteration and
+// neither a flush nor kUpdatePX has folded it.
 __global__ void __launch_bounds__(256) kFlushX(int64_t n, double* __restrict__ x64, float* __restrict__ x32,
-                                               const Scalars* S, int conditional) {
+                                               const float* __restrict__ p, Scalars* S, int conditional) {
     if (conditional && (S->done || !trueResidualDue(S))) return;
+    const bool pending =
+        conditional || (S->rStamp == S->matvecs && S->foldStamp != S->matvecs && S->pxStamp != S->matvecs);
+    const double a = pending ? S->alpha : 0.0;
     for (int64_t i = blockIdx.x * (int64_t)NT + threadIdx.x; i < n; i += (int64_t)gridDim.x * NT) {
-        x64[i] += (double)x32[i];
+        x64[i] += (double)x32[i] + a * (double)p[i];
         x32[i] = 0.f;
+    }
+    if (conditional && blockIdx.x == 0 && threadIdx.x == 0) S->foldStamp = S->matvecs;
+}
+
+// Mixed precision: p = z + beta p, and the deferred x += alpha p (old p) of
+// this iteration unless a flush has folded it.
+__global__ void __launch_bounds__(256) kUpdatePX(int64_t n, float* __restrict__ p, const float* __restrict__ z,
+                                                 float* __restrict__ x, Scalars* S) {
+    if (S->done) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) S->pxStamp = S->matvecs;  // read only by kFlushX
+    const float beta = (float)S->beta;
+    const float ax = S->foldStamp == S->matvecs ? 0.f : (float)S->alpha;
+    const int64_t tid = blockIdx.x * (int64_t)NT + threadIdx.x, stride = (int64_t)gridDim.x * NT;
+    const int64_t n4 = n / 4;
+    for (int64_t q = tid; q < n4; q += stride) {
+        float pv[4], zv[4], xv[4];
+        V4<float>::ld(p + 4 * q, pv);
+        V4<float>::ld(z + 4 * q, zv);
+        V4<float>::ld(x + 4 * q, xv);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            xv[k] = fma(ax, pv[k], xv[k]);
+            pv[k] = fma(beta, pv[k], zv[k]);
+        }
+        V4<float>::st(p + 4 * q, pv);
+        V4<float>::st(x + 4 * q, xv);
+    }
+    for (int64_t i = 4 * n4 + tid; i < n; i += stride) {
+        x[i] = fma(ax, p[i], x[i]);
+        p[i] = fma(beta, p[i], z[i]);
     }
 }
 
@@ -1412,6 +1641,7 @@ __global__ void kInitScalars(Scalars* S, double tol, long long maxIter, int flex
     s.mixed = mixed;
     s.replaceEvery = replaceEvery;
     s.delta2 = mixed ? delta * delta : 0.0;
+    s.rStamp = s.foldStamp = s.pxStamp = -1;
     *S = s;
 }
 
@@ -1506,7 +1736,23 @@ int launchProlongSmooth(const LaunchCtx& c, const Grid& gf, const Grid& gc, int 
                         const T* dinv, const uint8_t* flags, T* zf, double coef, int maskFixed, const T* aux, int epi,
                         int checkDone) {
     dim3 grid = nodeGrid(gf), block(32, 8);
-    if (div == 2) {
+    const int64_t flatBlocksN = (int64_t)prolongFlatRowGroups(gf) * gf.nz;
+    const size_t flatSmem = 2 * sizeof(T) * kProlongCoarseRows * 3 * (size_t)gc.nx;
+    if (div == 2 && flatBlocksN <= kMaxRedBlocks && flatSmem <= kProlongFlatMaxSmem) {
+        if (flatSmem > 48 * 1024) {
+            static std::once_flag once;
+            std::call_once(once, [] {
+                cudaFuncSetAttribute(kProlongFlat<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)kProlongFlatMaxSmem);
+            });
+        }
+        auto al = [](const void* q) { return ((uintptr_t)q & 15u) == 0; };
+        const int vec = al(rf) && al(dinv) && al(zf) && ((uintptr_t)flags & 3u) == 0;
+        kProlongFlat<T><<<(unsigned)flatBlocksN, 256, flatSmem, c.stream>>>(gf, gc, zc, rf, dinv, flags, zf, coef,
+                                                                             maskFixed, aux, epi, vec, 1.0f / gf.nx,
+                                                                             c.S, c.rb, checkDone);
+    } else if (div == 2) {
+        // grids beyond the flat kernel's block or shared-memory limits (over ~1000^3 nodes)
         dim3 cgrid((gc.nx + 31) / 32, (gc.ny + 7) / 8, (gc.nz + PZC - 1) / PZC);
         kProlongSmooth2<T><<<cgrid, block, 0, c.stream>>>(gf, gc, zc, rf, dinv, flags, zf, coef, maskFixed, aux, epi,
                                                           c.S, c.rb, checkDone);
@@ -1568,8 +1814,18 @@ int launchUpdateXR(const LaunchCtx& c, int64_t n, TX* x, TV* r, const TV* p, con
     return 1;
 }
 
-int launchFlushX(const LaunchCtx& c, int64_t n, double* x64, float* x32, int conditional) {
-    kFlushX<<<flatBlocks(n), NT, 0, c.stream>>>(n, x64, x32, c.S, conditional);
+int launchFlushX(const LaunchCtx& c, int64_t n, double* x64, float* x32, const float* p, int conditional) {
+    kFlushX<<<flatBlocks(n), NT, 0, c.stream>>>(n, x64, x32, p, c.S, conditional);
+    return 1;
+}
+
+int launchUpdateR(const LaunchCtx& c, int64_t n, float* r, const float* Ap) {
+    kUpdateR<<<flatBlocks(n), NT, 0, c.stream>>>(n, r, Ap, c.S, c.rb);
+    return 1;
+}
+
+int launchUpdatePX(const LaunchCtx& c, int64_t n, float* p, const float* z, float* x) {
+    kUpdatePX<<<flatBlocks(n), NT, 0, c.stream>>>(n, p, z, x, c.S);
     return 1;
 }
 

@@ -29,6 +29,9 @@ struct Scalars {
     int mixed;
     int replaceEvery;
     int pad;
+    // mixed precision, deferred x += alpha p: value of `matvecs` when kUpdateR
+    // last ran, when a conditional kFlushX folded alpha p, when kUpdatePX ran
+    long long rStamp, foldStamp, pxStamp;
 };
 
 struct RedBuf {
@@ -150,9 +153,13 @@ int launchPackSymHalf(cudaStream_t s, const float* K, int64_t n, float invScale,
 // x += alpha p ; r -= alpha Ap ; rr -> EPI_CONV
 template <typename TX, typename TV>
 int launchUpdateXR(const LaunchCtx& c, int64_t n, TX* x, TV* r, const TV* p, const TV* Ap);
-// x64 += x32; x32 = 0 (mixed precision).  conditional: only in iterations that
-// recompute the FP64 true residual.
-int launchFlushX(const LaunchCtx& c, int64_t n, double* x64, float* x32, int conditional);
+// x64 += x32 (+ the deferred alpha p); x32 = 0 (mixed precision).  conditional:
+// only in iterations that recompute the FP64 true residual.
+int launchFlushX(const LaunchCtx& c, int64_t n, double* x64, float* x32, const float* p, int conditional);
+// Mixed precision: r -= alpha Ap with r.r (x += alpha p deferred); p = z + beta p
+// with the deferred x += alpha p.
+int launchUpdateR(const LaunchCtx& c, int64_t n, float* r, const float* Ap);
+int launchUpdatePX(const LaunchCtx& c, int64_t n, float* p, const float* z, float* x);
 // p = z + beta p
 template <typename T>
 int launchUpdateP(const LaunchCtx& c, int64_t n, T* p, const T* z, int first);
