@@ -209,7 +209,8 @@ typedef enum vfem_kernel_class {
     VFEM_K_COARSE_FP64 = 10,
     VFEM_K_COARSE_FP32 = 11,
     VFEM_K_TRUE_RESIDUAL_DF = 12, /* f - K x on FP64 vectors in double-float arithmetic */
-    VFEM_K_COUNT = 13
+    VFEM_K_UPDATE_RESTRICT_MIXED = 13, /* mixed: r -= alpha Ap, r.r and the first restriction in one pass */
+    VFEM_K_COUNT = 14
 } vfem_kernel_class;
 
 /* Measurement helper (no counterpart in the reference): average device time in

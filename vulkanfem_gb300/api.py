@@ -50,7 +50,7 @@ EXPORTED = (
 
 KERNEL_CLASSES = ("matvec_fp64", "matvec_fp32", "restrict_fp64", "restrict_fp32", "prolong_fp64", "prolong_fp32",
                   "update_xr_fp64", "update_xr_mixed", "update_p_fp64", "update_p_fp32", "coarse_fp64",
-                  "coarse_fp32", "true_residual_df")
+                  "coarse_fp32", "true_residual_df", "update_restrict_mixed")
 
 
 class VfemError(RuntimeError):

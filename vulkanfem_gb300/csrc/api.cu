@@ -57,9 +57,10 @@ struct DevLevel {
 struct GraphKey {
     int mg, prec, flexible, pre, post, replace, chunk;
     double omega;
+    int parity;  // which buffer holds the level-0 residual when the chunk starts
     bool operator<(const GraphKey& o) const {
-        return std::tie(mg, prec, flexible, pre, post, replace, chunk, omega) <
-               std::tie(o.mg, o.prec, o.flexible, o.pre, o.post, o.replace, o.chunk, o.omega);
+        return std::tie(mg, prec, flexible, pre, post, replace, chunk, omega, parity) <
+               std::tie(o.mg, o.prec, o.flexible, o.pre, o.post, o.replace, o.chunk, o.omega, o.parity);
     }
 };
 
@@ -82,6 +83,7 @@ struct vfem_problem {
     double *f64 = nullptr, *x64 = nullptr, *p64 = nullptr, *Ap64 = nullptr;
     float *p32 = nullptr, *Ap32 = nullptr;
     float* x32 = nullptr;  // mixed precision: FP32 solution correction since the last FP64 flush
+    float* r32b = nullptr;  // mixed precision: the level-0 residual alternates between L[0].r32 and this
     // coarsest dense inverse
     int64_t nc = 0;
     int32_t* freeDof = nullptr;
@@ -159,7 +161,7 @@ void freeProblem(vfem_problem* p) {
         cudaFree(l.r64); cudaFree(l.z64); cudaFree(l.t64); cudaFree(l.r32); cudaFree(l.z32); cudaFree(l.t32);
     }
     cudaFree(p->f64); cudaFree(p->x64); cudaFree(p->p64); cudaFree(p->Ap64); cudaFree(p->p32); cudaFree(p->Ap32);
-    cudaFree(p->x32);
+    cudaFree(p->x32); cudaFree(p->r32b);
     cudaFree(p->freeDof); cudaFree(p->Kinv64); cudaFree(p->KinvH); cudaFree(p->cb64); cudaFree(p->cb32);
     cudaFree(p->KinvV64); cudaFree(p->KinvVH); cudaFree(p->dFreeNode); cudaFree(p->cpart);
     cudaFree(p->dFlag);
@@ -552,7 +554,7 @@ vfem_status createImpl(const uint8_t* vox, int nx, int ny, int nz, const double*
     }
     int64_t nv0 = p->L[0].nvec();
     CKP(dalloc(&p->f64, nv0)); CKP(dalloc(&p->x64, nv0)); CKP(dalloc(&p->p64, nv0)); CKP(dalloc(&p->Ap64, nv0));
-    CKP(dalloc(&p->p32, nv0)); CKP(dalloc(&p->Ap32, nv0)); CKP(dalloc(&p->x32, nv0));
+    CKP(dalloc(&p->p32, nv0)); CKP(dalloc(&p->Ap32, nv0)); CKP(dalloc(&p->x32, nv0)); CKP(dalloc(&p->r32b, nv0));
     CKP(dalloc(&p->S, 1));
     CKP(dalloc(&p->rb.partials, 2 * (int64_t)kMaxRedBlocks));
     CKP(dalloc(&p->rb.ticket, 1));
@@ -650,7 +652,8 @@ int matvecDF(vfem_problem* p, const MatvecArgs<double>& a) {
 // holding the result (it differs from z in the multiplicative cycle when the
 // number of post-sweeps is odd).
 template <typename T>
-int vcycle(vfem_problem* p, const vfem_options& o, int lv, T* r, T* z, T** outZ, const T* aux, int epi) {
+int vcycle(vfem_problem* p, const vfem_options& o, int lv, T* r, T* z, T** outZ, const T* aux, int epi,
+           bool restricted = false) {
     const int L = (int)p->L.size();
     int n = 0;
     DevLevel& l = p->L[lv];
@@ -666,7 +669,8 @@ int vcycle(vfem_problem* p, const vfem_options& o, int lv, T* r, T* z, T** outZ,
     DevLevel& lc = p->L[lv + 1];
     if (o.mg_mode == VFEM_MG_REFERENCE) {
         // Additive cycle of the reference (MultigridPreconditioner.hpp:158-193).
-        n += launchRestrict<T>(c, l.g, lc.g, lc.div, r, lvR<T>(lc), 1);
+        // restricted: the caller has already restricted r (fused residual update).
+        if (!restricted) n += launchRestrict<T>(c, l.g, lc.g, lc.div, r, lvR<T>(lc), 1);
         T* zc = nullptr;
         n += vcycle<T>(p, o, lv + 1, lvR<T>(lc), lvZ<T>(lc), &zc, nullptr, EPI_NONE);
         n += launchProlongSmooth<T>(c, l.g, lc.g, lc.div, zc, r, lvDinv<T>(l, false), l.flags, z, 2.0, lv == 0 ? 1 : 0,
@@ -721,7 +725,8 @@ int vcycle(vfem_problem* p, const vfem_options& o, int lv, T* r, T* z, T** outZ,
 
 // Preconditioner application on level 0 (identity when mg_mode == NONE).
 template <typename T>
-int precondition(vfem_problem* p, const vfem_options& o, T* r, T* z, T** outZ, const T* aux, int epi) {
+int precondition(vfem_problem* p, const vfem_options& o, T* r, T* z, T** outZ, const T* aux, int epi,
+                 bool restricted = false) {
     if (o.mg_mode == VFEM_MG_NONE) {
         DevLevel& l = p->L[0];
         int n = launchConvert<T, T>(p->stream, l.nvec(), r, z);
@@ -729,12 +734,19 @@ int precondition(vfem_problem* p, const vfem_options& o, T* r, T* z, T** outZ, c
         *outZ = z;
         return n;
     }
-    return vcycle<T>(p, o, 0, r, z, outZ, aux, epi);
+    return vcycle<T>(p, o, 0, r, z, outZ, aux, epi, restricted);
+}
+
+// The mixed solve fuses its residual update with the first restriction of the
+// reference cycle (2x first coarsening); the residual then alternates between
+// two buffers from iteration to iteration.
+bool fusedUpdateRestrict(const vfem_problem* p, const vfem_options& o) {
+    return o.precision == VFEM_PREC_MIXED && o.mg_mode == VFEM_MG_REFERENCE && p->L.size() >= 2 && p->L[1].div == 2;
 }
 
 // One PCG iteration (after initialisation).  FP64: Eigen's loop body.
 // Mixed: FP32 vectors, FP64 x, conditional FP64 true-residual pass.
-int iteration(vfem_problem* p, const vfem_options& o, double** zOut64, float** zOut32) {
+int iteration(vfem_problem* p, const vfem_options& o, double** zOut64, float** zOut32, int parity) {
     DevLevel& l0 = p->L[0];
     const int64_t n = l0.nvec();
     LaunchCtx c = ctx(p);
@@ -754,19 +766,30 @@ int iteration(vfem_problem* p, const vfem_options& o, double** zOut64, float** z
         a.dot0 = DOT_X_OUT;
         a.epi = EPI_ALPHA;
         k += matvec<float>(p, a);
-        k += launchUpdateR(c, n, l0.r32, p->Ap32);  // x += alpha p is deferred to launchUpdatePX / the flush
+        // x += alpha p is deferred to launchUpdatePX / the flush
+        const bool fused = fusedUpdateRestrict(p, o);
+        float* r = l0.r32;
+        if (fused) {
+            float* rIn = parity ? p->r32b : l0.r32;
+            r = parity ? l0.r32 : p->r32b;
+            k += launchUpdateRestrict(c, l0.g, p->L[1].g, rIn, p->Ap32, r, p->L[1].r32);
+        } else {
+            k += launchUpdateR(c, n, r, p->Ap32);
+        }
         k += launchFlushX(c, n, p->x64, p->x32, p->p32, 1);
         // True residual f - K x64 in double-float; only its FP32 rounding (the new
         // recursive residual) and its norm are kept.
         MatvecArgs<double> t = mvArgs<double>(p, 0, p->x64, nullptr, MV_RESID);
         t.f = p->f64;
-        t.y32 = l0.r32;
+        t.y32 = r;
         t.dot0 = DOT_OUT_OUT;
         t.epi = EPI_TRUE;
         t.condTrue = 1;
         k += matvecDF(p, t);
+        // a replaced residual is restricted again
+        if (fused) k += launchRestrict<float>(c, l0.g, p->L[1].g, 2, r, p->L[1].r32, 2);
         float* z = nullptr;
-        k += precondition<float>(p, o, l0.r32, l0.z32, &z, o.flexible ? p->Ap32 : nullptr, EPI_BETA);
+        k += precondition<float>(p, o, r, l0.z32, &z, o.flexible ? p->Ap32 : nullptr, EPI_BETA, fused);
         k += launchUpdatePX(c, n, p->p32, z, p->x32);
         *zOut32 = z;
     }
@@ -833,32 +856,44 @@ vfem_status solveImpl(vfem_problem* p, const vfem_options* optIn, bool haveX0, v
     CK(cudaGetLastError());
     // ---- chunked iterations replayed from a cached graph
     const int chunk = o.check_every;
-    GraphKey key{o.mg_mode, o.precision, o.flexible, o.pre_sweeps, o.post_sweeps, mixed ? o.replace_every : 0,
-                 o.check_every, o.omega};
-    CachedGraph& cg = p->graphs[key];
-    if (!cg.exec) {
-        cudaGraph_t graph = nullptr;
-        CK(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
-        long long k = 0;
-        for (int i = 0; i < chunk; ++i) k += iteration(p, o, &z64, &z32);
-        cudaError_t ec = cudaStreamEndCapture(p->stream, &graph);
-        if (ec != cudaSuccess) return fail(VFEM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ec));
-        ec = cudaGraphInstantiate(&cg.exec, graph, 0);
-        cudaGraphDestroy(graph);
-        if (ec != cudaSuccess) {
-            cg.exec = nullptr;
-            return fail(VFEM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ec));
+    // With the fused residual update the residual alternates between two buffers,
+    // so a chunk of odd length has a second graph for the other starting buffer.
+    const int flip = fusedUpdateRestrict(p, o) ? (chunk & 1) : 0;
+    auto graphFor = [&](int parity, CachedGraph** out) -> vfem_status {
+        GraphKey key{o.mg_mode, o.precision, o.flexible, o.pre_sweeps, o.post_sweeps, mixed ? o.replace_every : 0,
+                     o.check_every, o.omega, parity};
+        CachedGraph& cg = p->graphs[key];
+        if (!cg.exec) {
+            cudaGraph_t graph = nullptr;
+            CK(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
+            long long k = 0;
+            for (int i = 0; i < chunk; ++i) k += iteration(p, o, &z64, &z32, (parity + i) & 1);
+            cudaError_t ec = cudaStreamEndCapture(p->stream, &graph);
+            if (ec != cudaSuccess) return fail(VFEM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ec));
+            ec = cudaGraphInstantiate(&cg.exec, graph, 0);
+            cudaGraphDestroy(graph);
+            if (ec != cudaSuccess) {
+                cg.exec = nullptr;
+                return fail(VFEM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ec));
+            }
+            cg.kernels = k;
         }
-        cg.kernels = k;
-    }
+        *out = &cg;
+        return VFEM_OK;
+    };
+    CachedGraph* cgs[2] = {nullptr, nullptr};
+    if ((s = graphFor(0, &cgs[0])) != VFEM_OK) return s;
+    if (flip && (s = graphFor(1, &cgs[1])) != VFEM_OK) return s;
+    int parity = 0;  // the residual starts in L[0].r32
     long long chunks = 0;
     const long long maxChunks = maxIter / chunk + 2;
     for (;;) {
         CK(cudaMemcpyAsync(p->hS, p->S, sizeof(Scalars), cudaMemcpyDeviceToHost, p->stream));
         CK(cudaStreamSynchronize(p->stream));
         if (p->hS->done != RUNNING || chunks >= maxChunks) break;
-        CK(cudaGraphLaunch(cg.exec, p->stream));
-        launches += cg.kernels;
+        CK(cudaGraphLaunch(cgs[parity]->exec, p->stream));
+        launches += cgs[parity]->kernels;
+        parity ^= flip;
         ++chunks;
     }
     if (mixed) launches += launchFlushX(c, n, p->x64, p->x32, p->p32, 0);  // fold the remaining correction
@@ -1199,6 +1234,9 @@ vfem_status vfem_profile_kernels(vfem_problem* p, int32_t reps, double* ms) {
                     return two ? launchRestrict<double>(c, l0.g, l1.g, l1.div, l0.r64, l1.r64, 1) : 0;
                 case VFEM_K_RESTRICT_FP32:
                     return two ? launchRestrict<float>(c, l0.g, l1.g, l1.div, l0.r32, l1.r32, 1) : 0;
+                case VFEM_K_UPDATE_RESTRICT_MIXED:
+                    return two && l1.div == 2 ? launchUpdateRestrict(c, l0.g, l1.g, l0.r32, p->Ap32, p->r32b, l1.r32)
+                                              : 0;
                 case VFEM_K_PROLONG_FP64:
                     return two ? launchProlongSmooth<double>(c, l0.g, l1.g, l1.div, l1.z64, l0.r64, l0.dinv64, l0.flags,
                                                              l0.z64, 2.0, 1, nullptr, EPI_STORE, 1)

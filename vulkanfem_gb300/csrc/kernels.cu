@@ -129,6 +129,7 @@ __device__ void applyEpi(int epi, Scalars* S, double t0, double t1) {
             if (t0 == 0.0 || t1 < S->threshold) S->done = CONVERGED;
             break;
         case EPI_TRUE:
+            S->replStamp = S->matvecs;
             S->rrTrue = t0;
             S->rr = t0;
             S->rrLast = t0;
@@ -797,20 +798,34 @@ __global__ void __launch_bounds__(256) kRestrict(Grid gf, Grid gc, const T* __re
 // is kept for the next layer, and r(2cx-1) of a lane is r(2cx+1) of the lane
 // below (a warp shuffle), so each fine value is loaded about 1.5 times.
 constexpr int PZR = 4;
-template <typename T>
-__global__ void __launch_bounds__(256) kRestrict2(Grid gf, Grid gc, const T* __restrict__ rf, T* __restrict__ rc,
-                                                  const Scalars* S, int checkDone) {
+// UPD (mixed-precision CG): the residual update r -= alpha Ap of the finest
+// level fused in.  rf is the old residual and Ap the product; each thread
+// writes the updated values of the fine nodes its coarse cell owns (fine x, y,
+// z in {2c, 2c + 1}) to rOut (a different vector: neighbouring cells read
+// the old values of their halos) and sums their squares for r.r; halo values
+// (row 2cy-1, the block's first plane, the left x neighbour of lane 0) are
+// recomputed from rf and Ap.  checkDone = 2: run only in an iteration that
+// replaced the residual by the true one (restricting the replacement).
+template <typename T, bool UPD>
+__global__ void __launch_bounds__(256) kRestrict2(Grid gf, Grid gc, const T* __restrict__ rf, const T* __restrict__ Ap,
+                                                  T* __restrict__ rOut, T* __restrict__ rc, Scalars* S, RedBuf rb,
+                                                  int checkDone) {
     if (checkDone && S->done) return;
+    if (checkDone == 2 && S->replStamp != S->matvecs) return;
     const int lane = threadIdx.x;
     const int cx = blockIdx.x * 32 + lane, cy = blockIdx.y * 8 + threadIdx.y;
     const bool valid = cx < gc.nx && cy < gc.ny;
     const T half = T(0.5);
+    const T av = UPD ? (T)S->alpha : T(0);
     const int fx0 = 2 * cx;
+    DotAcc<T> acc;
     // Weighted plane sum at fine layer fz: the three rows 2cy-1 .. 2cy+1, each
     // r(2cx-1)/2 + r(2cx) + r(2cx+1)/2.  All loads of the plane are issued first,
     // then the shuffles; all lanes take part, out-of-grid fine nodes count 0.
-    auto planeSum = [&](int fz, T (&P)[3]) {
+    auto planeSum = [&](int fz, bool ownPlane, T (&P)[3]) {
         T c0[3][3], c1[3][3], cl[3][3];
+        int64_t bases[3];
+        bool ok0s[3], ok1s[3];
 #pragma unroll
         for (int r = 0; r < 3; ++r) {
             const int fy = 2 * cy - 1 + r;
@@ -818,12 +833,38 @@ __global__ void __launch_bounds__(256) kRestrict2(Grid gf, Grid gc, const T* __r
             const int64_t base = rowOk ? gf.store(0, fy, fz) : 0;
             const bool ok0 = rowOk && fx0 < gf.nx, ok1 = rowOk && fx0 + 1 < gf.nx;
             const bool okl = lane == 0 && rowOk && fx0 - 1 >= 0 && fx0 - 1 < gf.nx;
+            bases[r] = base;
+            ok0s[r] = ok0;
+            ok1s[r] = ok1;
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
                 c0[r][c] = ok0 ? rf[3 * (base + fx0) + c] : T(0);
                 c1[r][c] = ok1 ? rf[3 * (base + fx0 + 1) + c] : T(0);
                 cl[r][c] = okl ? rf[3 * (base + fx0 - 1) + c] : T(0);
+                if (UPD) {
+                    const T a0 = ok0 ? Ap[3 * (base + fx0) + c] : T(0);
+                    const T a1 = ok1 ? Ap[3 * (base + fx0 + 1) + c] : T(0);
+                    const T al = okl ? Ap[3 * (base + fx0 - 1) + c] : T(0);
+                    c0[r][c] = fma(-av, a0, c0[r][c]);
+                    c1[r][c] = fma(-av, a1, c1[r][c]);
+                    cl[r][c] = fma(-av, al, cl[r][c]);
+                }
             }
+        }
+        if (UPD && ownPlane && valid) {
+#pragma unroll
+            for (int r = 1; r < 3; ++r)
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    if (ok0s[r]) {
+                        rOut[3 * (bases[r] + fx0) + c] = c0[r][c];
+                        acc.add(c0[r][c] * c0[r][c]);
+                    }
+                    if (ok1s[r]) {
+                        rOut[3 * (bases[r] + fx0 + 1) + c] = c1[r][c];
+                        acc.add(c1[r][c] * c1[r][c]);
+                    }
+                }
         }
         T row[3][3];
 #pragma unroll
@@ -839,11 +880,11 @@ __global__ void __launch_bounds__(256) kRestrict2(Grid gf, Grid gc, const T* __r
     };
     const int cz0 = blockIdx.z * PZR, cz1 = min(gc.nz, cz0 + PZR);
     T Pm[3];
-    planeSum(2 * cz0 - 1, Pm);
+    planeSum(2 * cz0 - 1, false, Pm);
     for (int cz = cz0; cz < cz1; ++cz) {
         T P0[3], Pp[3];
-        planeSum(2 * cz, P0);
-        planeSum(2 * cz + 1, Pp);
+        planeSum(2 * cz, true, P0);
+        planeSum(2 * cz + 1, true, Pp);
         if (valid) {
             T* q = rc + 3 * gc.store(cx, cy, cz);
 #pragma unroll
@@ -851,6 +892,10 @@ __global__ void __launch_bounds__(256) kRestrict2(Grid gf, Grid gc, const T* __r
         }
 #pragma unroll
         for (int c = 0; c < 3; ++c) Pm[c] = Pp[c];
+    }
+    if (UPD) {
+        double v[1] = {acc.get()}, t[1];
+        if (gridReduce<256, 1>(v, rb, t)) applyEpi(EPI_CONV, S, t[0], 0.0);
     }
 }
 
@@ -1641,7 +1686,7 @@ __global__ void kInitScalars(Scalars* S, double tol, long long maxIter, int flex
     s.mixed = mixed;
     s.replaceEvery = replaceEvery;
     s.delta2 = mixed ? delta * delta : 0.0;
-    s.rStamp = s.foldStamp = s.pxStamp = -1;
+    s.rStamp = s.foldStamp = s.pxStamp = s.replStamp = -1;
     *S = s;
 }
 
@@ -1726,8 +1771,15 @@ int launchRestrict(const LaunchCtx& c, const Grid& gf, const Grid& gc, int div, 
         kRestrict<T, 4><<<nodeGrid(gc), block, 0, c.stream>>>(gf, gc, rf, rc, c.S, checkDone);
     } else {
         dim3 grid((gc.nx + 31) / 32, (gc.ny + 7) / 8, (gc.nz + PZR - 1) / PZR);
-        kRestrict2<T><<<grid, block, 0, c.stream>>>(gf, gc, rf, rc, c.S, checkDone);
+        kRestrict2<T, false><<<grid, block, 0, c.stream>>>(gf, gc, rf, nullptr, nullptr, rc, c.S, c.rb, checkDone);
     }
+    return 1;
+}
+
+int launchUpdateRestrict(const LaunchCtx& c, const Grid& gf, const Grid& gc, const float* rIn, const float* Ap,
+                         float* rOut, float* rc) {
+    dim3 block(32, 8), grid((gc.nx + 31) / 32, (gc.ny + 7) / 8, (gc.nz + PZR - 1) / PZR);
+    kRestrict2<float, true><<<grid, block, 0, c.stream>>>(gf, gc, rIn, Ap, rOut, rc, c.S, c.rb, 1);
     return 1;
 }
 

@@ -29,9 +29,10 @@ struct Scalars {
     int mixed;
     int replaceEvery;
     int pad;
-    // mixed precision, deferred x += alpha p: value of `matvecs` when kUpdateR
-    // last ran, when a conditional kFlushX folded alpha p, when kUpdatePX ran
-    long long rStamp, foldStamp, pxStamp;
+    // mixed precision, deferred x += alpha p: value of `matvecs` when the
+    // residual update last ran, when a conditional kFlushX folded alpha p, when
+    // kUpdatePX ran; replStamp: when the true residual last replaced r
+    long long rStamp, foldStamp, pxStamp, replStamp;
 };
 
 struct RedBuf {
@@ -102,6 +103,8 @@ int launchMatvec(const LaunchCtx& c, const MatvecArgs<T>& a, bool structured, co
 // ~48-bit significands): the mixed-precision true residual.  a.y may be null.
 int launchMatvecDF(const LaunchCtx& c, const MatvecArgs<double>& a, bool structured, const double* opconst);
 
+// checkDone: 1 = skip once the solve is done; 2 = also skip unless the true
+// residual replaced r in this iteration (2x coarsening only).
 template <typename T>
 int launchRestrict(const LaunchCtx& c, const Grid& gf, const Grid& gc, int div, const T* rf, T* rc,
                    int checkDone);
@@ -160,6 +163,11 @@ int launchFlushX(const LaunchCtx& c, int64_t n, double* x64, float* x32, const f
 // with the deferred x += alpha p.
 int launchUpdateR(const LaunchCtx& c, int64_t n, float* r, const float* Ap);
 int launchUpdatePX(const LaunchCtx& c, int64_t n, float* p, const float* z, float* x);
+// Mixed precision, reference cycle with a 2x first coarsening: the residual
+// update fused with the first restriction (rOut = rIn - alpha Ap, r.r, rc =
+// R rOut); rOut must not alias rIn.
+int launchUpdateRestrict(const LaunchCtx& c, const Grid& gf, const Grid& gc, const float* rIn, const float* Ap,
+                         float* rOut, float* rc);
 // p = z + beta p
 template <typename T>
 int launchUpdateP(const LaunchCtx& c, int64_t n, T* p, const T* z, int first);
