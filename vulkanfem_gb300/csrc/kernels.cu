@@ -554,6 +554,87 @@ __device__ __forceinline__ void fwht4x3(T (&v)[12]) {
     }
 }
 
+// FP32: the x and y components of a node move as one register pair through
+// the packed FP32x2 instructions (same IEEE results; p - r as fma(r, -1, p) is
+// exact before its rounding), the z component alone: 2/3 of the instructions.
+__device__ __forceinline__ float2 pr2(const float* v) { return make_float2(v[0], v[1]); }
+__device__ __forceinline__ void st2(float* v, float2 a) {
+    v[0] = a.x;
+    v[1] = a.y;
+}
+__device__ __forceinline__ float2 sub2(float2 p, float2 r) { return __ffma2_rn(r, make_float2(-1.f, -1.f), p); }
+__device__ __forceinline__ void bfly3(float* a, float* b) {
+    const float2 p = pr2(a), r = pr2(b);
+    st2(a, __fadd2_rn(p, r));
+    st2(b, sub2(p, r));
+    const float pz = a[2], rz = b[2];
+    a[2] = pz + rz;
+    b[2] = pz - rz;
+}
+template <>
+__device__ __forceinline__ void fwht4x3<float>(float (&v)[12]) {
+    bfly3(v, v + 3);
+    bfly3(v + 6, v + 9);
+    bfly3(v, v + 6);
+    bfly3(v + 3, v + 9);
+}
+
+// uh = (qb + qt, qb - qt) (24 values).
+template <typename T>
+__device__ __forceinline__ void sumDiff12(const T (&a)[12], const T (&b)[12], T (&u)[24]) {
+#pragma unroll
+    for (int i = 0; i < 12; ++i) {
+        u[i] = a[i] + b[i];
+        u[12 + i] = a[i] - b[i];
+    }
+}
+template <>
+__device__ __forceinline__ void sumDiff12<float>(const float (&a)[12], const float (&b)[12], float (&u)[24]) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const float2 p = pr2(a + 3 * q), r = pr2(b + 3 * q);
+        st2(u + 3 * q, __fadd2_rn(p, r));
+        st2(u + 12 + 3 * q, sub2(p, r));
+        u[3 * q + 2] = a[3 * q + 2] + b[3 * q + 2];
+        u[12 + 3 * q + 2] = a[3 * q + 2] - b[3 * q + 2];
+    }
+}
+// u[i] *= e for the modes 1..7 (i >= 3).
+template <typename T>
+__device__ __forceinline__ void scaleModes(T (&u)[24], T e) {
+#pragma unroll
+    for (int i = 3; i < 24; ++i) u[i] *= e;
+}
+template <>
+__device__ __forceinline__ void scaleModes<float>(float (&u)[24], float e) {
+#pragma unroll
+    for (int m = 1; m < 8; ++m) {
+        st2(u + 3 * m, __fmul2_rn(pr2(u + 3 * m), make_float2(e, e)));
+        u[3 * m + 2] *= e;
+    }
+}
+// nb = carry + (y_bottom + y_top); carry = y_bottom - y_top.
+template <typename T>
+__device__ __forceinline__ void foldCarry(const T (&y)[24], T (&carry)[12], T (&nb)[12]) {
+#pragma unroll
+    for (int i = 0; i < 12; ++i) {
+        nb[i] = carry[i] + (y[i] + y[12 + i]);
+        carry[i] = y[i] - y[12 + i];
+    }
+}
+template <>
+__device__ __forceinline__ void foldCarry<float>(const float (&y)[24], float (&carry)[12], float (&nb)[12]) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const float2 yb = pr2(y + 3 * q), yt = pr2(y + 12 + 3 * q), cr = pr2(carry + 3 * q);
+        st2(nb + 3 * q, __fadd2_rn(cr, __fadd2_rn(yb, yt)));
+        st2(carry + 3 * q, sub2(yb, yt));
+        const float zb = y[3 * q + 2], zt = y[12 + 3 * q + 2];
+        nb[3 * q + 2] = carry[3 * q + 2] + (zb + zt);
+        carry[3 * q + 2] = zb - zt;
+    }
+}
+
 // The structured (isotropic cube) product with the Walsh-Hadamard factors
 // shared along z.  With corner a = (q, dz) and mode m = (mq, mz), the 8-point
 // transform splits into the 4-point transforms Q_0, Q_1 of the element's bottom
@@ -675,19 +756,10 @@ __global__ void __launch_bounds__(MV_TX* MV_TY, sizeof(TC) == 4 ? 3 : 2)
         if (Ee != 0.f) {
             TC uh[24], yh[24];
             const TC e = sc * TC(Ee);
-#pragma unroll
-            for (int i = 0; i < 12; ++i) {
-                uh[i] = qb[i] + qt[i];
-                uh[12 + i] = qb[i] - qt[i];
-            }
-#pragma unroll
-            for (int i = 3; i < 24; ++i) uh[i] *= e;
+            sumDiff12<TC>(qb, qt, uh);
+            scaleModes<TC>(uh, e);
             applyKhat<TC>(uh, yh, kp);
-#pragma unroll
-            for (int i = 0; i < 12; ++i) {
-                nb[i] = carry[i] + (yh[i] + yh[12 + i]);
-                carry[i] = yh[i] - yh[12 + i];
-            }
+            foldCarry<TC>(yh, carry, nb);
         } else {
 #pragma unroll
             for (int i = 0; i < 12; ++i) {
