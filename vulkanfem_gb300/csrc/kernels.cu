@@ -1470,25 +1470,29 @@ __global__ void __launch_bounds__(256) kSymTile(const __half* __restrict__ tiles
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int tc = lane & 15, tr = warp * 2 + (lane >> 4);
     const __half* K = tiles + t * (CT * CT);
-    T bJ[4], bI[4], rs[4], cs[4];
+    // Products in packed FP32x2: a row sum keeps its even and odd columns in
+    // the two halves of one register pair, a column pair shares one pair.
+    const float2 bJ01 = make_float2(b[J * CT + 4 * tc], b[J * CT + 4 * tc + 1]);
+    const float2 bJ23 = make_float2(b[J * CT + 4 * tc + 2], b[J * CT + 4 * tc + 3]);
+    T bI[4], rs[4], cs[4];
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        bJ[j] = b[J * CT + 4 * tc + j];
-        bI[j] = b[I * CT + 4 * tr + j];
-        rs[j] = cs[j] = T(0);
-    }
+    for (int j = 0; j < 4; ++j) bI[j] = b[I * CT + 4 * tr + j];
+    float2 cs01 = make_float2(0.f, 0.f), cs23 = make_float2(0.f, 0.f);
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
         const uint2 raw = *reinterpret_cast<const uint2*>(K + (4 * tr + i) * CT + 4 * tc);
         const float2 k01 = __half22float2(*reinterpret_cast<const __half2*>(&raw.x));
         const float2 k23 = __half22float2(*reinterpret_cast<const __half2*>(&raw.y));
-        const T k[4] = {k01.x, k01.y, k23.x, k23.y};
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            rs[i] = fma(k[j], bJ[j], rs[i]);
-            cs[j] = fma(k[j], bI[i], cs[j]);
-        }
+        const float2 r2 = __ffma2_rn(k23, bJ23, __fmul2_rn(k01, bJ01));
+        rs[i] = r2.x + r2.y;
+        const float2 bi = make_float2(bI[i], bI[i]);
+        cs01 = __ffma2_rn(k01, bi, cs01);
+        cs23 = __ffma2_rn(k23, bi, cs23);
     }
+    cs[0] = cs01.x;
+    cs[1] = cs01.y;
+    cs[2] = cs23.x;
+    cs[3] = cs23.y;
 #pragma unroll
     for (int o = 1; o < 16; o <<= 1)
 #pragma unroll
