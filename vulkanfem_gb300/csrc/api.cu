@@ -49,6 +49,10 @@ struct DevLevel {
     float* dinv32 = nullptr;
     double* dinvR64 = nullptr;
     float* dinvR32 = nullptr;
+    // The reference cycle's inverse diagonal for the mixed V-cycle: FP16 values
+    // times dinvHScale (a power of two mapping the largest entry into (2^13, 2^14]).
+    __half* dinvH = nullptr;
+    float dinvHScale = 1.0f;
     double *r64 = nullptr, *z64 = nullptr, *t64 = nullptr;
     float *r32 = nullptr, *z32 = nullptr, *t32 = nullptr;
     int64_t nvec() const { return 3 * g.nnode; }
@@ -157,7 +161,7 @@ void freeProblem(vfem_problem* p) {
     for (auto& l : p->L) {
         if (l.Ev != l.E) cudaFree(l.Ev);
         cudaFree(l.E); cudaFree(l.flags); cudaFree(l.nodeStore);
-        cudaFree(l.dinv64); cudaFree(l.dinv32); cudaFree(l.dinvR64); cudaFree(l.dinvR32);
+        cudaFree(l.dinv64); cudaFree(l.dinv32); cudaFree(l.dinvR64); cudaFree(l.dinvR32); cudaFree(l.dinvH);
         cudaFree(l.r64); cudaFree(l.z64); cudaFree(l.t64); cudaFree(l.r32); cudaFree(l.z32); cudaFree(l.t32);
     }
     cudaFree(p->f64); cudaFree(p->x64); cudaFree(p->p64); cudaFree(p->Ap64); cudaFree(p->p32); cudaFree(p->Ap32);
@@ -398,9 +402,11 @@ vfem_status buildHierarchyDevice(vfem_problem* p, const std::vector<LevelPlan>& 
     float* dEin = nullptr;
     double* dtab = nullptr;
     int64_t* dfixed = nullptr;
+    unsigned* dmax = nullptr;
     vfem_status result = VFEM_OK;
     auto cleanup = [&]() {
         cudaFree(dcnt); cudaFree(scratch); cudaFree(dvox); cudaFree(dEin); cudaFree(dtab); cudaFree(dfixed);
+        cudaFree(dmax);
     };
 #define CKS(call)                                                                                        \
     do {                                                                                                 \
@@ -429,7 +435,7 @@ vfem_status buildHierarchyDevice(vfem_problem* p, const std::vector<LevelPlan>& 
         CKS(dalloc(&d.E, nn));
         CKS(dalloc(&d.flags, nn));
         CKS(dalloc(&d.dinv64, nv)); CKS(dalloc(&d.dinv32, nv));
-        CKS(dalloc(&d.dinvR64, nv)); CKS(dalloc(&d.dinvR32, nv));
+        CKS(dalloc(&d.dinvR64, nv)); CKS(dalloc(&d.dinvR32, nv)); CKS(dalloc(&d.dinvH, nv));
         SetupCounters* c = dcnt + i;
         if (i == 0) {
             d.Ev = d.E;
@@ -483,6 +489,23 @@ vfem_status buildHierarchyDevice(vfem_problem* p, const std::vector<LevelPlan>& 
                               d.dinv64, d.dinv32));
         }
         CKS(gpuDiagRedisc(st, d.g, d.Ev, d.flags, d.scale, dg, d.dinvR64, d.dinvR32));
+        {
+            // FP16 copy of dinv32: the smoothing term of the mixed V-cycle reads 2
+            // bytes per value instead of 4 (a relative rounding of 2^-11 on a
+            // Jacobi step of the preconditioner).
+            if (!dmax) CKS(dalloc(&dmax, 1));
+            CKS(cudaMemsetAsync(dmax, 0, sizeof(unsigned), st));
+            p->launches += launchMaxAbs(st, d.dinv32, nv, dmax);
+            unsigned bits = 0;
+            CKS(cudaMemcpyAsync(&bits, dmax, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+            CKS(cudaStreamSynchronize(st));
+            float mx = 0.0f;
+            std::memcpy(&mx, &bits, sizeof(float));
+            int e = 0;
+            if (mx > 0.0f && std::isfinite(mx)) std::frexp(mx, &e);
+            d.dinvHScale = std::ldexp(1.0f, e - 14);
+            p->launches += launchToHalf(st, d.dinv32, nv, 1.0f / d.dinvHScale, d.dinvH);
+        }
         p->launches += 8;
     }
     CKS(cudaStreamSynchronize(st));
@@ -595,6 +618,11 @@ template <>
 double* lvT<double>(DevLevel& l) { return l.t64; }
 template <>
 float* lvT<float>(DevLevel& l) { return l.t32; }
+// The mixed V-cycle's smoothing reads the FP16 inverse diagonal.
+template <typename T>
+HalfDiag halfDiag(const DevLevel& l) {
+    return std::is_same<T, float>::value ? HalfDiag{l.dinvH, l.dinvHScale} : HalfDiag();
+}
 template <typename T>
 T* lvDinv(DevLevel& l, bool redisc);
 template <>
@@ -674,7 +702,7 @@ int vcycle(vfem_problem* p, const vfem_options& o, int lv, T* r, T* z, T** outZ,
         T* zc = nullptr;
         n += vcycle<T>(p, o, lv + 1, lvR<T>(lc), lvZ<T>(lc), &zc, nullptr, EPI_NONE);
         n += launchProlongSmooth<T>(c, l.g, lc.g, lc.div, zc, r, lvDinv<T>(l, false), l.flags, z, 2.0, lv == 0 ? 1 : 0,
-                                    lv == 0 ? aux : nullptr, lv == 0 ? epi : EPI_NONE, 1);
+                                    lv == 0 ? aux : nullptr, lv == 0 ? epi : EPI_NONE, 1, halfDiag<T>(l));
         *outZ = z;
         return n;
     }
@@ -1243,7 +1271,7 @@ vfem_status vfem_profile_kernels(vfem_problem* p, int32_t reps, double* ms) {
                                : 0;
                 case VFEM_K_PROLONG_FP32:
                     return two ? launchProlongSmooth<float>(c, l0.g, l1.g, l1.div, l1.z32, l0.r32, l0.dinv32, l0.flags,
-                                                            l0.z32, 2.0, 1, nullptr, EPI_STORE, 1)
+                                                            l0.z32, 2.0, 1, nullptr, EPI_STORE, 1, halfDiag<float>(l0))
                                : 0;
                 case VFEM_K_UPDATE_XR_FP64:
                     return launchUpdateXR<double, double>(c, n, p->x64, l0.r64, p->p64, p->Ap64);

@@ -1247,9 +1247,33 @@ __device__ __forceinline__ void cpAsync(T* dst, const T* src) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(d), "l"(src), "n"(sizeof(T)) : "memory");
 }
 
+// Inverse-diagonal values of a chunk: T, or FP16 (scaled; 8-byte loads).
+__device__ __forceinline__ float diagVal(__half h) { return __half2float(h); }
+__device__ __forceinline__ float diagVal(float v) { return v; }
+__device__ __forceinline__ double diagVal(double v) { return v; }
 template <typename T>
+__device__ __forceinline__ void ldDiag12(const T* p, T (&v)[12]) {
+#pragma unroll
+    for (int q = 0; q < 3; ++q) V4<T>::ld(p + 4 * q, *reinterpret_cast<T(*)[4]>(v + 4 * q));
+}
+__device__ __forceinline__ void ldDiag12(const __half* p, float (&v)[12]) {
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        const uint2 raw = reinterpret_cast<const uint2*>(p)[q];
+        const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&raw.x));
+        const float2 b = __half22float2(*reinterpret_cast<const __half2*>(&raw.y));
+        v[4 * q] = a.x;
+        v[4 * q + 1] = a.y;
+        v[4 * q + 2] = b.x;
+        v[4 * q + 3] = b.y;
+    }
+}
+
+// DT: the type the inverse diagonal is stored in (T, or FP16 scaled so that
+// coef already carries the scale).
+template <typename T, typename DT>
 __global__ void __launch_bounds__(256)
-    kProlongFlat(Grid gf, Grid gc, const T* __restrict__ zc, const T* __restrict__ rf, const T* __restrict__ dinv,
+    kProlongFlat(Grid gf, Grid gc, const T* __restrict__ zc, const T* __restrict__ rf, const DT* __restrict__ dinv,
                  const uint8_t* __restrict__ flags, T* __restrict__ zf, double coef, int maskFixed,
                  const T* __restrict__ aux, int epi, int vec, float invNx, Scalars* S, RedBuf rb, int checkDone) {
     if (checkDone && S->done) return;
@@ -1349,8 +1373,8 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
                 for (int v = 0; v < 3; ++v) {
                     V4<T>::ld(rf + 3 * n0 + 4 * v, *reinterpret_cast<T(*)[4]>(rv + 4 * v));
-                    V4<T>::ld(dinv + 3 * n0 + 4 * v, *reinterpret_cast<T(*)[4]>(dv + 4 * v));
                 }
+                ldDiag12(dinv + 3 * n0, dv);
                 fl4 = *reinterpret_cast<const uint32_t*>(flags + n0);
             } else {
 #pragma unroll
@@ -1359,7 +1383,7 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
                     for (int c = 0; c < 3; ++c) {
                         rv[3 * t + c] = in ? rf[3 * (n0 + t) + c] : T(0);
-                        dv[3 * t + c] = in ? dinv[3 * (n0 + t) + c] : T(0);
+                        dv[3 * t + c] = in ? (T)diagVal(dinv[3 * (n0 + t) + c]) : T(0);
                     }
                     if (in) fl4 |= (uint32_t)flags[n0 + t] << (8 * t);
                 }
@@ -1436,6 +1460,21 @@ __global__ void kPackSymHalf(const float* __restrict__ K, int64_t n, int64_t nb,
         const int64_t row = I * CT + e / CT, col = J * CT + e % CT;
         tiles[i] = __float2half_rn((row < n && col < n) ? K[row * n + col] * invScale : 0.0f);
     }
+}
+
+// *out = max |x_i| as FP32 bits (non-negative floats order like their bits); *out zeroed by the caller.
+__global__ void __launch_bounds__(256) kMaxAbs(const float* __restrict__ x, int64_t n, unsigned* __restrict__ out) {
+    float m = 0.0f;
+    for (int64_t i = blockIdx.x * (int64_t)NT + threadIdx.x; i < n; i += (int64_t)gridDim.x * NT) m = fmaxf(m, fabsf(x[i]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(m));
+}
+
+__global__ void __launch_bounds__(256) kToHalf(const float* __restrict__ x, int64_t n, float invScale,
+                                               __half* __restrict__ y) {
+    for (int64_t i = blockIdx.x * (int64_t)NT + threadIdx.x; i < n; i += (int64_t)gridDim.x * NT)
+        y[i] = __float2half_rn(x[i] * invScale);
 }
 
 // Largest diagonal entry of a row-major n x n matrix (one block).
@@ -1862,23 +1901,28 @@ int launchUpdateRestrict(const LaunchCtx& c, const Grid& gf, const Grid& gc, con
 template <typename T>
 int launchProlongSmooth(const LaunchCtx& c, const Grid& gf, const Grid& gc, int div, const T* zc, const T* rf,
                         const T* dinv, const uint8_t* flags, T* zf, double coef, int maskFixed, const T* aux, int epi,
-                        int checkDone) {
+                        int checkDone, HalfDiag hd) {
     dim3 grid = nodeGrid(gf), block(32, 8);
     const int64_t flatBlocksN = (int64_t)prolongFlatRowGroups(gf) * gf.nz;
     const size_t flatSmem = 2 * sizeof(T) * kProlongCoarseRows * 3 * (size_t)gc.nx;
     if (div == 2 && flatBlocksN <= kMaxRedBlocks && flatSmem <= kProlongFlatMaxSmem) {
-        if (flatSmem > 48 * 1024) {
-            static std::once_flag once;
-            std::call_once(once, [] {
-                cudaFuncSetAttribute(kProlongFlat<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)kProlongFlatMaxSmem);
-            });
-        }
         auto al = [](const void* q) { return ((uintptr_t)q & 15u) == 0; };
-        const int vec = al(rf) && al(dinv) && al(zf) && ((uintptr_t)flags & 3u) == 0;
-        kProlongFlat<T><<<(unsigned)flatBlocksN, 256, flatSmem, c.stream>>>(gf, gc, zc, rf, dinv, flags, zf, coef,
-                                                                             maskFixed, aux, epi, vec, 1.0f / gf.nx,
-                                                                             c.S, c.rb, checkDone);
+        const bool half = std::is_same<T, float>::value && hd.d != nullptr;
+        const int vec = al(rf) && al(zf) && ((uintptr_t)flags & 3u) == 0 &&
+                        (half ? ((uintptr_t)hd.d & 7u) == 0 : al(dinv));
+        auto go = [&](auto kern, const auto* dptr, double cf) {
+            if (flatSmem > 48 * 1024)
+                cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kProlongFlatMaxSmem);
+            kern<<<(unsigned)flatBlocksN, 256, flatSmem, c.stream>>>(gf, gc, zc, rf, dptr, flags, zf, cf, maskFixed, aux,
+                                                                     epi, vec, 1.0f / gf.nx, c.S, c.rb, checkDone);
+        };
+        if constexpr (std::is_same<T, float>::value) {
+            if (half) {
+                go(kProlongFlat<float, __half>, hd.d, coef * (double)hd.scale);
+                return 1;
+            }
+        }
+        go(kProlongFlat<T, T>, dinv, coef);
     } else if (div == 2) {
         // grids beyond the flat kernel's block or shared-memory limits (over ~1000^3 nodes)
         dim3 cgrid((gc.nx + 31) / 32, (gc.ny + 7) / 8, (gc.nz + PZC - 1) / PZC);
@@ -1923,6 +1967,16 @@ int launchCoarseSolve(const LaunchCtx& c, CoarseInv<T> Kinv, int64_t n, const in
         kSymReduce<<<(unsigned)nb, 1024, 0, c.stream>>>(part, nb, n, freeDof, Kinv.scale, zc, c.S, checkDone);
         return 3;
     }
+}
+
+int launchMaxAbs(cudaStream_t s, const float* x, int64_t n, unsigned* outBits) {
+    kMaxAbs<<<flatBlocks(n), NT, 0, s>>>(x, n, outBits);
+    return 1;
+}
+
+int launchToHalf(cudaStream_t s, const float* x, int64_t n, float invScale, __half* y) {
+    kToHalf<<<flatBlocks(n), NT, 0, s>>>(x, n, invScale, y);
+    return 1;
 }
 
 int launchMaxDiag(cudaStream_t s, const float* K, int64_t n, float* out) {
@@ -2097,7 +2151,7 @@ cudaError_t launchMatvecNoAlloc(cudaStream_t s, const MatvecArgs<double>& a, boo
     template int launchMatvec<T>(const LaunchCtx&, const MatvecArgs<T>&, bool, const void*);                         \
     template int launchRestrict<T>(const LaunchCtx&, const Grid&, const Grid&, int, const T*, T*, int);               \
     template int launchProlongSmooth<T>(const LaunchCtx&, const Grid&, const Grid&, int, const T*, const T*,          \
-                                        const T*, const uint8_t*, T*, double, int, const T*, int, int);              \
+                                        const T*, const uint8_t*, T*, double, int, const T*, int, int, HalfDiag);    \
     template int launchJacobiZero<T>(const LaunchCtx&, const Grid&, const T*, const T*, const uint8_t*, T*, double,  \
                                      int);                                                                           \
     template int launchProlongAdd<T>(const LaunchCtx&, const Grid&, const Grid&, int, const T*, const uint8_t*, T*,  \

@@ -110,11 +110,16 @@ int launchRestrict(const LaunchCtx& c, const Grid& gf, const Grid& gc, int div, 
                    int checkDone);
 
 // Reference-mode up-leg: zf = used ? P zc + coef * dinv o rf : 0 (fixed -> 0 on level 0),
-// optional dots r.z and z.aux with epilogue `epi`.
+// optional dots r.z and z.aux with epilogue `epi`.  hd (FP32, 2x coarsening):
+// the inverse diagonal as FP16 values times a power of two, read instead of dinv.
+struct HalfDiag {
+    const __half* d = nullptr;
+    float scale = 1.0f;
+};
 template <typename T>
 int launchProlongSmooth(const LaunchCtx& c, const Grid& gf, const Grid& gc, int div, const T* zc, const T* rf,
                         const T* dinv, const uint8_t* flags, T* zf, double coef, int maskFixed,
-                        const T* aux, int epi, int checkDone);
+                        const T* aux, int epi, int checkDone, HalfDiag hd = HalfDiag());
 
 // V-cycle helpers: z = mask(omega dinv r); zf += mask(P zc).
 template <typename T>
@@ -146,6 +151,9 @@ struct CoarseInv<float> {
 template <typename T>
 int launchCoarseSolve(const LaunchCtx& c, CoarseInv<T> Kinv, int64_t n, const int32_t* freeDof, const T* rc, T* tmp,
                       T* part, T* zc, int checkDone);
+// *outBits = max |x_i| as FP32 bits (zero *outBits first); y = FP16(x * invScale).
+int launchMaxAbs(cudaStream_t s, const float* x, int64_t n, unsigned* outBits);
+int launchToHalf(cudaStream_t s, const float* x, int64_t n, float invScale, __half* y);
 // *out = the largest diagonal entry of a row-major n x n matrix.
 int launchMaxDiag(cudaStream_t s, const float* K, int64_t n, float* out);
 // Pack a full symmetric row-major n x n matrix, times invScale, into
