@@ -2,18 +2,22 @@
 //
 // Kernel map (reference shader / routine it replaces, paths relative to the
 // reference project root):
-//   kMatvec          MatxVec.comp + FixedNodes.comp + VecDotVec.comp
+//   kMatvecH, kMatvec  MatxVec.comp + FixedNodes.comp + VecDotVec.comp
 //                    (MatrixFreeSparse.hpp:197-214): atomic-free element-by-element
-//                    product on a 2.5-D tile, fixed rows zeroed, dots fused.
-//   kRestrict        CWiseMult.comp + Restrict.comp (MultigridPreconditioner.hpp:67-108):
-//                    full weighting on the dense grid, one thread per coarse node.
-//   kProlongSmooth   Interpolate.comp + PreSmoothAndAXPY.comp + Smooth.comp
-//                    (MultigridPreconditioner.hpp:110-155,176-181), fixed mask and r.z fused.
-//   kCoarseGather/kSymTile/kSymReduce  the coarsest SimplicialLDLT solve
+//                    product on a 2.5-D tile (kMatvecH: Walsh-factorised isotropic
+//                    cube Ke; kMatvec: general Ke), fixed rows zeroed, dots fused.
+//   kRestrict2, kRestrict  CWiseMult.comp + Restrict.comp (MultigridPreconditioner.hpp:67-108):
+//                    full weighting on the dense grid (kRestrict2<T, true> also
+//                    performs the mixed solve's residual update, ConjugateGradient_1.comp).
+//   kProlongFlat, kProlongSmooth2, kProlongSmooth  Interpolate.comp + PreSmoothAndAXPY.comp +
+//                    Smooth.comp (MultigridPreconditioner.hpp:110-155,176-181),
+//                    fixed mask and r.z fused.
+//   kCoarseGather/kSymTile/kSymReduce, kGemv64  the coarsest SimplicialLDLT solve
 //                    (MultigridPreconditioner.hpp:174-175) as a dense symmetric
-//                    inverse, stored as half its tiles, applied on the device.
-//   kUpdateXR        ConjugateGradient_1.comp + VecDotVec.comp (r.r).
-//   kUpdateP         ConjugateGradient_2.comp.
+//                    inverse: FP16 packed half tiles (mixed) or the full FP64 matrix.
+//   kUpdateXR, kUpdateR  ConjugateGradient_1.comp + VecDotVec.comp (r.r).
+//   kUpdateP, kUpdatePX  ConjugateGradient_2.comp (kUpdatePX: with the mixed solve's
+//                    deferred x update).
 // Reductions are deterministic: block partials in a fixed grid, summed in a
 // fixed order by the last block to finish (no floating-point atomics).
 #include <cfloat>
