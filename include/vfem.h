@@ -180,6 +180,11 @@ vfem_status vfem_apply_operator_device_noalloc(vfem_problem* p, const double* x_
  * V-cycle of `mg_mode` (VFEM_MG_REFERENCE or VFEM_MG_VCYCLE) in FP64. */
 vfem_status vfem_apply_preconditioner(vfem_problem* p, int32_t mg_mode, const double* r, double* z);
 
+/* The same V-cycle as the mixed-precision solver applies it (no counterpart in
+ * the reference): FP32 vectors, FP16 coarsest inverse tiles and, in the
+ * reference cycle, an FP16 inverse diagonal; r and z in FP64. */
+vfem_status vfem_apply_preconditioner_mixed(vfem_problem* p, int32_t mg_mode, const double* r, double* z);
+
 /* MultigridPreconditioner::restrict / interpolate (MultigridPreconditioner.hpp:67-155)
  * between `level` (fine) and `level + 1` (coarse), compressed numbering of each
  * level. */

@@ -40,6 +40,7 @@ EXPORTED = (
     "vfem_options_default", "vfem_status_string", "vfem_hex8_stiffness", "vfem_problem_create",
     "vfem_problem_destroy", "vfem_problem_info", "vfem_problem_set_loads", "vfem_problem_set_rhs",
     "vfem_solve", "vfem_solve_device", "vfem_apply_operator", "vfem_apply_preconditioner",
+    "vfem_apply_preconditioner_mixed",
     "vfem_restrict", "vfem_interpolate", "vfem_inverse_diagonal", "vfem_fixed_nodes",
     "vfem_kernel_launch_count", "vfem_last_error_message", "vfem_profile_kernels",
     "vfem_apply_operator_device_noalloc",
@@ -121,6 +122,7 @@ def load_library(build_if_missing=True):
     lib.vfem_solve_device.argtypes = [P, ctypes.POINTER(Options), ctypes.c_void_p, ctypes.POINTER(Stats)]
     lib.vfem_apply_operator.argtypes = [P, f64p, f64p]
     lib.vfem_apply_preconditioner.argtypes = [P, i32, f64p, f64p]
+    lib.vfem_apply_preconditioner_mixed.argtypes = [P, i32, f64p, f64p]
     lib.vfem_restrict.argtypes = [P, i32, f64p, f64p]
     lib.vfem_interpolate.argtypes = [P, i32, f64p, f64p]
     lib.vfem_inverse_diagonal.argtypes = [P, i32, f64p]
@@ -327,8 +329,12 @@ class MultigridPreconditioner:
     """``Eigen::MultigridPreconditioner`` (include/MultigridPreconditioner.hpp:12-214):
     ``compute(A)`` then ``solve(b)`` applies one V-cycle in FP64."""
 
-    def __init__(self, A=None, mode="reference"):
+    def __init__(self, A=None, mode="reference", precision="fp64"):
+        """precision "mixed": the V-cycle as the mixed-precision solver applies it."""
         self.mode = MG_MODES[mode]
+        if precision not in ("fp64", "mixed"):
+            raise VfemError(1, "precision must be 'fp64' or 'mixed'")
+        self.precision = precision
         self.A = None
         if A is not None:
             self.compute(A)
@@ -350,7 +356,9 @@ class MultigridPreconditioner:
         if b.size != self.A.rows():
             raise VfemError(1, "invalid number of rows of the right hand side")
         z = np.empty_like(b)
-        _check(self.A._lib.vfem_apply_preconditioner(self.A._h, self.mode, b, z))
+        fn = (self.A._lib.vfem_apply_preconditioner_mixed if self.precision == "mixed"
+              else self.A._lib.vfem_apply_preconditioner)
+        _check(fn(self.A._h, self.mode, b, z))
         return z
 
 

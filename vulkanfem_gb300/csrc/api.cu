@@ -1190,6 +1190,31 @@ vfem_status vfem_apply_preconditioner(vfem_problem* p, int32_t mg_mode, const do
     return fromDenseHost(p, 0, zo, z);
 }
 
+vfem_status vfem_apply_preconditioner_mixed(vfem_problem* p, int32_t mg_mode, const double* r, double* z) {
+    if (!p || !r || !z || (mg_mode != VFEM_MG_REFERENCE && mg_mode != VFEM_MG_VCYCLE))
+        return fail(VFEM_ERR_INVALID_ARGUMENT, "bad argument");
+    CK(cudaSetDevice(p->device));
+    DevLevel& l0 = p->L[0];
+    vfem_status s = ensureCoarse<float>(p, mg_mode == VFEM_MG_VCYCLE);
+    if (s != VFEM_OK) return s;
+    s = toDenseHost(p, 0, r, l0.r64, false);
+    if (s != VFEM_OK) return s;
+    vfem_options o;
+    vfem_options_default(&o);
+    o.mg_mode = mg_mode;
+    o.precision = VFEM_PREC_MIXED;
+    const int64_t n = l0.nvec();
+    int k = launchConvert<double, float>(p->stream, n, l0.r64, l0.r32);
+    k += launchInitScalars(p->stream, p->S, 1e-6, 1, 0, 1, 0, 0.0);
+    float* zo = nullptr;
+    k += vcycle<float>(p, o, 0, l0.r32, l0.z32, &zo, nullptr, EPI_NONE);
+    k += launchConvert<float, double>(p->stream, n, zo, l0.z64);
+    p->launches += k;
+    g_launches += k;
+    CK(cudaGetLastError());
+    return fromDenseHost(p, 0, l0.z64, z);
+}
+
 vfem_status vfem_restrict(vfem_problem* p, int32_t level, const double* fine, double* coarse) {
     if (!p || !fine || !coarse || level < 0 || level + 1 >= (int)p->L.size())
         return fail(VFEM_ERR_INVALID_ARGUMENT, "bad argument");
