@@ -47,10 +47,11 @@ WORKLOADS = {
                   "128^3 seeded Gaussian random field (sigma 6 voxels) at 40% fill, grounded component, "
                   "z=0 fixed, unit -z top load, 4 MG levels"),
     "porous384": (lambda: __import__("vulkanfem_gb300.domains", fromlist=["x"]).porous(384, 0.45, 6.0, seed=0,
-                                                                                        levels=6,
+                                                                                        levels=5,
                                                                                         lognormal_sigma=0.5),
                   "384^3 seeded Gaussian random field (sigma 6 voxels) at 45% fill, grounded component, "
-                  "E ~ lognormal(0,0.5), z=0 fixed, unit -z top load, 6 MG levels (coarsest 12^3 elements)"),
+                  "E ~ lognormal(0,0.5), z=0 fixed, unit -z top load, 5 MG levels (coarsest 24^3 elements, "
+                  "45,006 free DOFs)"),
     "cantilever": (lambda: __import__("vulkanfem_gb300.domains", fromlist=["x"]).cantilever(32, 16, 16, 3),
                    "32x16x16 solid cantilever, x=0 fixed, unit -z load on x=32, 3 MG levels"),
 }

@@ -71,7 +71,7 @@ def build(force=False, verbose=False, extra_flags=()):
                 print(msg)
     if force or jobs or _stale(LIB, objs):
         tmp = LIB + ".tmp%d" % os.getpid()
-        cmd = [nv] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcusolver", "-lcudart"]
+        cmd = [nv] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcusolver", "-lcublas", "-lcudart"]
         run(cmd)
         os.replace(tmp, LIB)
     return LIB

@@ -10,6 +10,7 @@
 // and stopping rule are Eigen 3.4's (x0 = 0, stop when |r|^2 < tol^2 |b|^2 on the
 // recursive residual, iterations counted without the breaking pass).
 #include <cuda_runtime.h>
+#include <cublas_v2.h>
 #include <cusolverDn.h>
 
 #include <algorithm>
@@ -34,7 +35,8 @@ namespace {
 std::atomic<long long> g_launches{0};
 thread_local std::string g_lastError;
 
-constexpr int64_t kMaxCoarseFree = 32768;
+constexpr int64_t kMaxCoarseFree = 65536;  // dense coarsest inverse: 16 GB in FP32 at the limit
+constexpr int64_t kMaxCoarse32 = 32768;    // above: the 64-bit cuSOLVER path (n^2 >= 2^31)
 
 struct DevLevel {
     Grid g;
@@ -259,6 +261,79 @@ struct SolverOf<float> {
 // FEM.cpp:19-63,498-513): assembled on the GPU in T, cuSOLVER Cholesky (potrf)
 // and inverse (potri) in T, symmetrised.  The FP32 inverse is factorised in
 // FP32 (tens of milliseconds instead of seconds for the FP64 one on GB300).
+// Coarsest systems beyond the 32-bit solver API (n^2 >= 2^31 values): 64-bit
+// Cholesky (cusolverDnXpotrf), triangular inverse of the factor
+// (cusolverDnXtrtri) and Kinv = L^-T L^-1 as one rank-n update (cuBLAS syrk,
+// 64-bit sizes) into `work`, then copied back to K (lower triangle in cuSOLVER's
+// column-major order; the caller symmetrises).
+template <typename T>
+vfem_status invertCoarseLarge(vfem_problem* p, T* K, int64_t n, cusolverDnHandle_t h) {
+    const cudaDataType dt = std::is_same<T, double>::value ? CUDA_R_64F : CUDA_R_32F;
+    cusolverDnParams_t params = nullptr;
+    cublasHandle_t hb = nullptr;
+    void* dws = nullptr;
+    int* info = nullptr;
+    T* C = nullptr;
+    vfem_status st = VFEM_OK;
+    size_t wd1 = 0, wh1 = 0, wd2 = 0, wh2 = 0;
+    if (cusolverDnCreateParams(&params) != CUSOLVER_STATUS_SUCCESS || cublasCreate(&hb) != CUBLAS_STATUS_SUCCESS)
+        st = fail(VFEM_ERR_CUDA, "cusolver/cublas handle");
+    if (st == VFEM_OK) cublasSetStream(hb, p->stream);
+    if (st == VFEM_OK &&
+        (cusolverDnXpotrf_bufferSize(h, params, CUBLAS_FILL_MODE_LOWER, n, dt, K, n, dt, &wd1, &wh1) !=
+             CUSOLVER_STATUS_SUCCESS ||
+         cusolverDnXtrtri_bufferSize(h, CUBLAS_FILL_MODE_LOWER, CUBLAS_DIAG_NON_UNIT, n, dt, K, n, &wd2, &wh2) !=
+             CUSOLVER_STATUS_SUCCESS))
+        st = fail(VFEM_ERR_CUDA, "cusolver 64-bit buffer size query failed");
+    std::vector<char> hws(std::max<size_t>(1, std::max(wh1, wh2)));
+    if (st == VFEM_OK && (cudaMalloc(&dws, std::max<size_t>(16, std::max(wd1, wd2))) != cudaSuccess ||
+                          cudaMalloc(&info, sizeof(int)) != cudaSuccess || dalloc(&C, n * n) != cudaSuccess))
+        st = fail(VFEM_ERR_OUT_OF_MEMORY, "coarse inverse workspace");
+    auto checkInfo = [&](const char* what) {
+        int hinfo = 0;
+        cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, p->stream);
+        if (cudaStreamSynchronize(p->stream) != cudaSuccess) return fail(VFEM_ERR_CUDA, what);
+        if (hinfo != 0)
+            return fail(VFEM_ERR_SINGULAR, std::string(what) + " (info " + std::to_string(hinfo) + ")");
+        return VFEM_OK;
+    };
+    if (st == VFEM_OK) {
+        if (cusolverDnXpotrf(h, params, CUBLAS_FILL_MODE_LOWER, n, dt, K, n, dt, dws, wd1, hws.data(), wh1, info) !=
+            CUSOLVER_STATUS_SUCCESS)
+            st = fail(VFEM_ERR_CUDA, "cusolverDnXpotrf failed");
+        else
+            st = checkInfo("coarsest system is not positive definite");
+    }
+    if (st == VFEM_OK) {
+        if (cusolverDnXtrtri(h, CUBLAS_FILL_MODE_LOWER, CUBLAS_DIAG_NON_UNIT, n, dt, K, n, dws, wd2, hws.data(), wh2,
+                             info) != CUSOLVER_STATUS_SUCCESS)
+            st = fail(VFEM_ERR_CUDA, "cusolverDnXtrtri failed");
+        else
+            st = checkInfo("coarsest factor inverse failed");
+    }
+    if (st == VFEM_OK) {
+        // syrk reads the whole of L^-1: clear its (column-major) upper triangle first
+        p->launches += launchZeroStrictRowMajorLower<T>(p->stream, K, n);
+        const T one = T(1), zero = T(0);
+        cublasStatus_t bs;
+        if constexpr (std::is_same<T, double>::value)
+            bs = cublasDsyrk_64(hb, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, n, n, &one, K, n, &zero, C, n);
+        else
+            bs = cublasSsyrk_64(hb, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, n, n, &one, K, n, &zero, C, n);
+        if (bs != CUBLAS_STATUS_SUCCESS) st = fail(VFEM_ERR_CUDA, "cublas syrk failed");
+        else if (cudaMemcpyAsync(K, C, sizeof(T) * (size_t)(n * n), cudaMemcpyDeviceToDevice, p->stream) !=
+                 cudaSuccess)
+            st = fail(VFEM_ERR_CUDA, "coarse inverse copy");
+    }
+    if (cudaStreamSynchronize(p->stream) != cudaSuccess && st == VFEM_OK) st = fail(VFEM_ERR_CUDA, "coarse inverse");
+    cudaFree(dws);
+    cudaFree(info);
+    cudaFree(C);
+    if (hb) cublasDestroy(hb);
+    if (params) cusolverDnDestroyParams(params);
+    return st;
+}
+
 template <typename T>
 vfem_status invertCoarse(vfem_problem* p, const float* E, double scale, T* K) {
     typedef typename SolverOf<T>::type Sv;
@@ -267,6 +342,17 @@ vfem_status invertCoarse(vfem_problem* p, const float* E, double scale, T* K) {
     CK(cudaMemsetAsync(K, 0, sizeof(T) * (size_t)(n * n), p->stream));
     p->launches += launchAssembleCoarse<T>(p->stream, dc.g, E, p->dFreeNode, p->ke.Ke, scale, K, n);
     CK(cudaGetLastError());
+    if (n > kMaxCoarse32) {
+        cusolverDnHandle_t hl = nullptr;
+        if (cusolverDnCreate(&hl) != CUSOLVER_STATUS_SUCCESS) return fail(VFEM_ERR_CUDA, "cusolverDnCreate failed");
+        cusolverDnSetStream(hl, p->stream);
+        vfem_status sl = invertCoarseLarge<T>(p, K, n, hl);
+        cusolverDnDestroy(hl);
+        if (sl != VFEM_OK) return sl;
+        p->launches += launchSymmetrizeLowerToFull<T>(p->stream, K, n);
+        if (cudaStreamSynchronize(p->stream) != cudaSuccess) return fail(VFEM_ERR_CUDA, "coarse inverse kernels");
+        return VFEM_OK;
+    }
     cusolverDnHandle_t h = nullptr;
     if (cusolverDnCreate(&h) != CUSOLVER_STATUS_SUCCESS) return fail(VFEM_ERR_CUDA, "cusolverDnCreate failed");
     cusolverDnSetStream(h, p->stream);

@@ -2070,6 +2070,20 @@ int launchAssembleCoarse(cudaStream_t s, const Grid& g, const float* E, const in
 }
 
 template <typename T>
+__global__ void kZeroStrictRowMajorLower(T* K, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n * n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = i / n, c = i - r * n;
+        if (c < r) K[i] = T(0);
+    }
+}
+
+template <typename T>
+int launchZeroStrictRowMajorLower(cudaStream_t s, T* K, int64_t n) {
+    kZeroStrictRowMajorLower<T><<<flatBlocks(n * n), NT, 0, s>>>(K, n);
+    return 1;
+}
+
+template <typename T>
 int launchSymmetrizeLowerToFull(cudaStream_t s, T* K, int64_t n) {
     kSymmetrize<T><<<flatBlocks(n * n), NT, 0, s>>>(K, n);
     return 1;
@@ -2169,7 +2183,8 @@ cudaError_t launchMatvecNoAlloc(cudaStream_t s, const MatvecArgs<double>& a, boo
     template int launchGatherCompressed<T>(cudaStream_t, int64_t, const int32_t*, const T*, double*);               \
     template int launchAssembleCoarse<T>(cudaStream_t, const Grid&, const float*, const int32_t*, const double*,     \
                                          double, T*, int64_t);                                                       \
-    template int launchSymmetrizeLowerToFull<T>(cudaStream_t, T*, int64_t);
+    template int launchSymmetrizeLowerToFull<T>(cudaStream_t, T*, int64_t);                                          \
+    template int launchZeroStrictRowMajorLower<T>(cudaStream_t, T*, int64_t);
 INST_T(double)
 INST_T(float)
 template int launchUpdateXR<double, double>(const LaunchCtx&, int64_t, double*, double*, const double*, const double*);

@@ -204,6 +204,10 @@ int launchAssembleCoarse(cudaStream_t s, const Grid& g, const float* E, const in
                          double scale, T* K, int64_t n);
 template <typename T>
 int launchSymmetrizeLowerToFull(cudaStream_t s, T* K, int64_t n);
+// Zero the strict lower triangle of a row-major n x n matrix (cuSOLVER's
+// column-major upper triangle).
+template <typename T>
+int launchZeroStrictRowMajorLower(cudaStream_t s, T* K, int64_t n);
 
 // Solver scalar initialisation (device side, so it can live in a graph).
 int launchInitScalars(cudaStream_t s, Scalars* S, double tol, long long maxIter, int flexible, int mixed,
