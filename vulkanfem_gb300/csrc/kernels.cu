@@ -2188,8 +2188,6 @@ cudaError_t launchMatvecNoAlloc(cudaStream_t s, const MatvecArgs<double>& a, boo
 INST_T(double)
 INST_T(float)
 template int launchUpdateXR<double, double>(const LaunchCtx&, int64_t, double*, double*, const double*, const double*);
-template int launchUpdateXR<double, float>(const LaunchCtx&, int64_t, double*, float*, const float*, const float*);
-template int launchUpdateXR<float, float>(const LaunchCtx&, int64_t, float*, float*, const float*, const float*);
 template int launchConvert<double, float>(cudaStream_t, int64_t, const double*, float*);
 template int launchConvert<float, double>(cudaStream_t, int64_t, const float*, double*);
 template int launchConvert<double, double>(cudaStream_t, int64_t, const double*, double*);

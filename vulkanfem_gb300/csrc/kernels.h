@@ -161,7 +161,7 @@ int launchMaxDiag(cudaStream_t s, const float* K, int64_t n, float* out);
 int launchPackSymHalf(cudaStream_t s, const float* K, int64_t n, float invScale, __half* tiles);
 
 // CG vector updates on flat arrays of length n.
-// x += alpha p ; r -= alpha Ap ; rr -> EPI_CONV
+// x += alpha p ; r -= alpha Ap ; rr -> EPI_CONV (FP64 solver: TX = TV = double)
 template <typename TX, typename TV>
 int launchUpdateXR(const LaunchCtx& c, int64_t n, TX* x, TV* r, const TV* p, const TV* Ap);
 // x64 += x32 (+ the deferred alpha p); x32 = 0 (mixed precision).  conditional:
