@@ -233,17 +233,22 @@ def run_reference_arm(args, dom, ws, rank):
     }
 
 
-def cpu_baseline(args, dom):
+def cpu_baseline(args, dom, threads=None, iters=None):
+    """The CPU restatement of the reference path on the host cores (all of them by
+    default; threads=1 is the reference's serial Eigen product), timed over a
+    bounded number of PCG iterations of the same workload."""
     import oracle
     from vulkanfem_gb300 import domains
-    threads = os.cpu_count() or 1
+    threads = threads or os.cpu_count() or 1
+    iters = iters or args.cpu_iters
     o = oracle.Oracle(dom.voxels, domains.hex8_stiffness(), dom.fixed, dom.num_levels, 0, threads=threads, E=dom.E)
     f = o.load_vector(dom.load_nodes, dom.load_values)
     t = time.perf_counter()
-    _, it, _ = o.pcg(f, tol=1e-6, iter_cap=args.cpu_iters)
+    _, it, _ = o.pcg(f, tol=1e-6, iter_cap=iters)
     dt = time.perf_counter() - t
     return {"value": o.num_dofs(0) * it / dt / 1e6, "unit": "MDOF/s", "cores": threads, "kind": "port",
-            "sample": "%d PCG iterations of the CPU restatement on the same workload (%.1f s)" % (it, dt)}
+            "sample": "%d PCG iterations of the CPU restatement on the same workload, %d thread(s) (%.1f s)"
+                      % (it, threads, dt)}
 
 
 def main():
@@ -331,9 +336,13 @@ def main():
         cst = [A.solve_device(**copts)[1] for _ in range(max(1, args.compare_steps))]
         cs = sum(s["solve_ms"] for s in cst) / 1e3 / len(cst)
         ci = sum(s["iterations"] for s in cst) / len(cst)
+        # the answers themselves (untimed solves that read the solution back)
+        u_main, _ = A.solve_device(want_solution=True, **sopts)
+        u_comp, _ = A.solve_device(want_solution=True, **copts)
         comp = {"solver": args.compare, "time_to_rtol_s": cs, "iterations": ci,
                 "mdof_s": dof * ci / cs / 1e6, "rel_residual": cst[-1]["rel_residual"],
-                "speedup_time_to_rtol": cs / (dev_s / len(stats))}
+                "speedup_time_to_rtol": cs / (dev_s / len(stats)),
+                "rel_l2_vs_%s" % args.compare: float(np.linalg.norm(u_main - u_comp) / np.linalg.norm(u_comp))}
 
     # ---- roofline of the dominant kernel (CUDA events on the library stream)
     ms = api.profile_kernels(A, args.profile_reps)
@@ -366,13 +375,19 @@ def main():
             "algorithmic_bytes": abytes, "ms_per_launch": kms, "peak_source": peak_src,
             "kernel_ms": ms}
 
+    o_full = api.make_options(**sopts)
+    solver_options = {k: getattr(o_full, k) for k, _ in api.Options._fields_ if k != "reserved"}
     line = {
         "metric": "MDOF/s (DOF x PCG iterations / solve time, rtol 1e-6 MG-PCG)",
         "value": value, "unit": "MDOF/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * tmax / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64" if mixed else "f64", "data": "synthetic",
         "config": {"workload": args.workload, "description": WORKLOADS[args.workload][1], "dofs": dof,
-                   "solver": args.solver, "solver_options": sopts, "parallelism": "replicas%d" % ws,
+                   "solver": args.solver, "solver_options": solver_options,
+                   "residual_replacement": "reliable updates (replace when |r| fell 20x since the last "
+                                           "replacement, and on a convergence claim) instead of every 50 "
+                                           "iterations: same iterations, fewer FP64-accurate products",
+                   "parallelism": "replicas%d" % ws,
                    "l2": "inputs larger than L2 (vectors %.0f MB each)" % (g0["nodes"] * 3 * s / 1e6)},
         "e2e": {"value": e2e, "unit": "MDOF/s", "h2d_bytes_per_step": 8 * dof, "d2h_bytes_per_step": 8 * dof},
         "gpu_launches": launches,
@@ -388,6 +403,7 @@ def main():
     }
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args, dom)
+        line["cpu_baseline_serial"] = cpu_baseline(args, dom, threads=1, iters=1)
     elif rank == 0:
         line["cpu_baseline"] = None
     if rank == 0:

@@ -84,7 +84,14 @@ typedef struct vfem_options {
                                 factor since the last replacement (reliable updates); default 0.05,
                                 0 = off.  A recursive residual that claims convergence is always
                                 replaced and re-checked. */
-    int32_t reserved[6];
+    int32_t fallback_fp64;   /* mixed precision: when the mixed solve ends in VFEM_ERR_BREAKDOWN, or
+                                stops short of rtol (stagnating true residual, or max_iter), plain
+                                FP64 MG-PCG continues from its iterate (from 0 if that iterate is not
+                                finite) with the iterations left of max_iter; default 1 */
+    int32_t debug_break_at;  /* testing: the solve's p^T A p at this iteration (1-based) is taken
+                                as -1, a forced VFEM_ERR_BREAKDOWN (a fallback phase does not
+                                inherit it); default 0 = off */
+    int32_t reserved[4];
 } vfem_options;
 
 typedef struct vfem_stats {
@@ -97,7 +104,9 @@ typedef struct vfem_stats {
     double h2d_ms, d2h_ms;   /* copies inside vfem_solve */
     int64_t kernel_launches; /* kernels launched by this call */
     int32_t status;          /* vfem_status of the solve */
-    int32_t reserved[7];
+    int32_t fallback;        /* 1: the mixed solve failed and plain FP64 MG-PCG continued (fallback_fp64) */
+    int64_t fallback_iterations; /* iterations of that FP64 phase (included in `iterations`) */
+    int32_t reserved[4];
 } vfem_stats;
 
 /* Fill `opt` with the defaults listed above. */
@@ -153,26 +162,27 @@ vfem_status vfem_solve_device(vfem_problem* p, const vfem_options* opt, double* 
 vfem_status vfem_apply_operator(vfem_problem* p, const double* x, double* y);
 
 /* No counterpart in the reference.  The operator product of vfem_apply_operator
- * for callers that cannot allocate GPU memory at the point of the call: code
- * running while a stream is captured into a CUDA graph (cudaMalloc is not
- * allowed there), hosts that hand every byte of device memory to their own pool
- * up front, and loops that must not stall on cudaMalloc's implicit device
- * synchronisation.  It calls no cudaMalloc, cudaFree or allocating library
- * routine.  The caller passes device arrays: x_device and y_device hold 3
- * doubles per node of the full node grid, (nx+1)*(ny+1)*(nz+1) nodes, x
- * fastest (the grid index replaces the compressed node id; values of x at
- * unused nodes are ignored, and y is written at every grid node, 0 at unused
- * nodes and fixed rows), and xKx_device receives
- * x.(Kx) in FP64.  Work is enqueued on `stream` (a cudaStream_t; NULL = the
- * default stream); the call returns without synchronising.
+ * for callers that cannot allocate GPU memory at the point of the call: hosts
+ * that hand every byte of device memory to their own pool up front (a solver
+ * framework or plugin that owns the device), and loops that must not stall on
+ * cudaMalloc's implicit device synchronisation.  It calls no cudaMalloc,
+ * cudaFree or allocating library routine.  The caller passes device arrays:
+ * x_device and y_device hold 3 doubles per node of the full node grid,
+ * (nx+1)*(ny+1)*(nz+1) nodes, x fastest (the grid index replaces the compressed
+ * node id).  Values of x at unused nodes are ignored, even non-finite ones; y is
+ * written at every grid node, 0 at unused nodes and fixed rows; xKx_device
+ * receives x.(Kx) in FP64, summed over the used, free nodes.  Work is enqueued on
+ * `stream` (a cudaStream_t; NULL = the default stream); the call returns without
+ * synchronising.
  * Scratch: a fixed 1,049,600-byte device array inside the library (reduction
- * partials for up to 65,536 blocks of the product, i.e. node grids up to about
- * 600^3); larger grids are rejected with VFEM_ERR_INVALID_ARGUMENT.  Every GPU
- * that loads the library holds the array until the process exits.  All calls
- * share it and it keeps the last call's contents; each call clears what must
- * start at zero, but calls that overlap on the GPU race.  The first call on a
- * device looks up the array's device address: make that first call before any
- * stream capture. */
+ * partials for up to 65,536 product blocks of 31 x 7 x 32 nodes, i.e. node grids
+ * up to about 760^3 for a cube); larger grids are rejected with
+ * VFEM_ERR_INVALID_ARGUMENT.  Every GPU that loads the library holds the array
+ * until the process exits.  All calls share it and it keeps the last call's
+ * contents; each call clears what must start at zero, but calls that overlap on
+ * the GPU race.  The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current: make that first call before
+ * any stream capture. */
 vfem_status vfem_apply_operator_device_noalloc(vfem_problem* p, const double* x_device, double* y_device,
                                                double* xKx_device, void* stream);
 

@@ -117,16 +117,19 @@ def test_fp64_solve_parity(case):
 
 
 def test_mixed_precision_solve(case):
+    """The mixed-precision solve against the reference's CPU path (the oracle's
+    FP64 MG-PCG at the same rtol 1e-6): true relative residual < 1e-6 and
+    displacement within 1e-5 relative L2 (measured 3e-10 .. 1e-7)."""
     o, A, f = case["o"], case["A"], case["f"]
-    x_tight, _, _ = o.pcg(f, tol=1e-10)
+    x_o, _, _ = o.pcg(f, tol=1e-6)
     u, st = A.solve(f, precision="mixed")
-    assert st["rel_residual"] < 1e-6
+    assert st["rel_residual"] < 1e-6 and st["fallback"] == 0
     r = f - o.matvec(u)
     rr = np.linalg.norm(r) / np.linalg.norm(f)
     assert rr < 1e-6
     # the reported residual is the double-float f - K x: the oracle's FP64 value to 1e-4 relative
     assert abs(st["rel_residual"] - rr) < 1e-4 * rr
-    assert rel(u, x_tight) < 1e-4
+    assert rel(u, x_o) < 1e-5
     # warm start from the answer: the double-float initial residual is already converged
     u2, st2 = A.solve(f, u0=u, precision="mixed")
     assert st2["iterations"] <= 1 and st2["rel_residual"] < 1e-6
@@ -136,13 +139,16 @@ def test_mixed_precision_solve(case):
 
 
 def test_vcycle_mode_solve(case):
+    """The multiplicative cycle has no reference counterpart: its answer at rtol
+    1e-6 must still match the reference path's answer to 1e-5 relative L2."""
     o, A, f = case["o"], case["A"], case["f"]
-    x_tight, _, _ = o.pcg(f, tol=1e-10)
+    x_o, _, _ = o.pcg(f, tol=1e-6)
     u, st = A.solve(f, mg_mode="vcycle")
     assert st["rel_residual"] < 1e-6
-    assert rel(u, x_tight) < 1e-4
+    assert rel(u, x_o) < 1e-5
     u2, st2 = A.solve(f, mg_mode="vcycle", precision="mixed", flexible=True)
     assert st2["rel_residual"] < 1e-6
+    assert rel(u2, x_o) < 1e-5
 
 
 def test_warm_start_and_repeat(case):

@@ -1,12 +1,15 @@
 """GPU test of vfem_apply_operator_device_noalloc, the operator product for
-callers that cannot allocate GPU memory at the call site (inside stream
-capture, under a host-owned memory pool, in loops that must not hit
-cudaMalloc's device synchronisation).
+callers that cannot allocate GPU memory at the call site (hosts whose own
+memory pool owns the device memory, loops that must not hit cudaMalloc's
+device synchronisation).
 
 Its result must equal the regular entry point vfem_apply_operator (same
 tolerance as the other operator parity tests, 1e-11 relative), on two calls
-in a row, since the calls share the library's fixed scratch array.  The device
-buffers below are the caller's (allocated by torch here, as a host pool would).
+in a row, since the calls share the library's fixed scratch array.  The second
+call puts NaN into x at the unused nodes, which the entry point documents as
+ignored, and checks that free device memory is the same before and after it.
+The device buffers below are the caller's (allocated by torch here, as a host
+pool would).
 """
 import ctypes
 
@@ -45,16 +48,22 @@ def test_noalloc_product_matches_apply_operator_twice():
         x = rng.standard_normal(A.rows())
         y_ref = A @ x                                   # the existing entry point
         xd = np.zeros(mask.shape + (3,))
+        if call == 1:
+            xd[~mask] = np.nan                          # ignored: no element touches these nodes
         xd[mask] = x.reshape(-1, 3)
         tx = torch.from_numpy(xd.reshape(-1)).cuda()
         ty = torch.full_like(tx, float("nan"))
         tdot = torch.full((1,), float("nan"), dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        free_before = torch.cuda.mem_get_info()[0]
         s = lib.vfem_apply_operator_device_noalloc(A._h, ctypes.c_void_p(tx.data_ptr()),
                                                    ctypes.c_void_p(ty.data_ptr()),
                                                    ctypes.c_void_p(tdot.data_ptr()),
                                                    ctypes.c_void_p(stream.cuda_stream))
         assert s == 0, api.STATUS_NAMES.get(s, s)
         torch.cuda.synchronize()
+        if call == 1:                                   # after the first call's one-time set-up
+            assert torch.cuda.mem_get_info()[0] == free_before
         yd = ty.cpu().numpy().reshape(mask.shape + (3,))
         y = yd[mask].reshape(-1)
         assert np.isfinite(yd).all()

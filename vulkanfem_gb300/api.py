@@ -67,7 +67,8 @@ class Options(ctypes.Structure):
         ("precision", ctypes.c_int32), ("omega", ctypes.c_double), ("pre_sweeps", ctypes.c_int32),
         ("post_sweeps", ctypes.c_int32), ("replace_every", ctypes.c_int32), ("flexible", ctypes.c_int32),
         ("check_every", ctypes.c_int32), ("compute_true_residual", ctypes.c_int32),
-        ("replace_delta", ctypes.c_double), ("reserved", ctypes.c_int32 * 6),
+        ("replace_delta", ctypes.c_double), ("fallback_fp64", ctypes.c_int32), ("debug_break_at", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 4),
     ]
 
 
@@ -76,7 +77,8 @@ class Stats(ctypes.Structure):
         ("iterations", ctypes.c_int64), ("matvecs", ctypes.c_int64), ("residual_replacements", ctypes.c_int64),
         ("rel_residual", ctypes.c_double), ("recursive_rel_residual", ctypes.c_double),
         ("solve_ms", ctypes.c_double), ("h2d_ms", ctypes.c_double), ("d2h_ms", ctypes.c_double),
-        ("kernel_launches", ctypes.c_int64), ("status", ctypes.c_int32), ("reserved", ctypes.c_int32 * 7),
+        ("kernel_launches", ctypes.c_int64), ("status", ctypes.c_int32), ("fallback", ctypes.c_int32),
+        ("fallback_iterations", ctypes.c_int64), ("reserved", ctypes.c_int32 * 4),
     ]
 
     def as_dict(self):
@@ -164,7 +166,7 @@ def hex8_stiffness(E=1.0, nu=0.3):
 
 def make_options(rtol=1e-6, max_iter=0, mg_mode="reference", precision="fp64", omega=0.6, pre_sweeps=1,
                  post_sweeps=1, replace_every=0, flexible=False, check_every=8, compute_true_residual=True,
-                 replace_delta=0.05):
+                 replace_delta=0.05, fallback_fp64=True, debug_break_at=0):
     lib = load_library()
     o = Options()
     lib.vfem_options_default(ctypes.byref(o))
@@ -180,6 +182,8 @@ def make_options(rtol=1e-6, max_iter=0, mg_mode="reference", precision="fp64", o
     o.check_every = check_every
     o.compute_true_residual = int(bool(compute_true_residual))
     o.replace_delta = replace_delta
+    o.fallback_fp64 = int(bool(fallback_fp64))
+    o.debug_break_at = int(debug_break_at)
     return o
 
 

@@ -17,6 +17,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <string>
@@ -35,8 +36,28 @@ namespace {
 std::atomic<long long> g_launches{0};
 thread_local std::string g_lastError;
 
-constexpr int64_t kMaxCoarseFree = 65536;  // dense coarsest inverse: 16 GB in FP32 at the limit
+// Dense coarsest inverse.  Peak device memory while it is built, at the limit
+// n = 65,536: the mixed solver's FP32 matrix (17.2 GB), the syrk result of the
+// 64-bit path (another 17.2 GB) and the FP16 tiles (8.6 GB), about 43 GB; an
+// FP64 inverse on that path needs 34.4 GB for the matrix plus 34.4 GB for the
+// syrk result (the FP32 one's memory is released by then, its FP16 tiles stay).
+constexpr int64_t kMaxCoarseFree = 65536;
 constexpr int64_t kMaxCoarse32 = 32768;    // above: the 64-bit cuSOLVER path (n^2 >= 2^31)
+
+// Testing hooks, read from the environment when a problem is created:
+//   VFEM_COARSE_64BIT_MIN=n   coarsest systems with more than n free DOFs take
+//                             the 64-bit factorisation path (default 32768);
+//   VFEM_FAULT_ALLOC_AT=k     the k-th device allocation of the set-up (1-based)
+//                             fails as if the device were out of memory.
+thread_local int64_t g_coarse64Min = kMaxCoarse32;
+thread_local long long g_allocCountdown = 0;
+long long envInt(const char* name, long long dflt) {
+    const char* v = std::getenv(name);
+    if (!v || !*v) return dflt;
+    char* end = nullptr;
+    const long long x = std::strtoll(v, &end, 10);
+    return (end && *end == 0) ? x : dflt;
+}
 
 struct DevLevel {
     Grid g;
@@ -141,18 +162,29 @@ vfem_status fail(vfem_status s, const std::string& msg) {
         }                                                                                          \
     } while (0)
 
+// Zeroed device allocation.  The memset runs on the legacy default stream, which
+// the problem's non-blocking stream does not wait for, so it is completed here:
+// otherwise a set-up kernel could see the previous owner's bytes of a recycled
+// block (a stale error flag, for example).
 template <typename T>
 cudaError_t dalloc(T** p, int64_t n) {
+    if (g_allocCountdown > 0 && --g_allocCountdown == 0) return cudaErrorMemoryAllocation;  // testing hook
     cudaError_t e = cudaMalloc((void**)p, (size_t)std::max<int64_t>(n, 1) * sizeof(T));
     if (e != cudaSuccess) return e;
-    return cudaMemset(*p, 0, (size_t)std::max<int64_t>(n, 1) * sizeof(T));
+    e = cudaMemset(*p, 0, (size_t)std::max<int64_t>(n, 1) * sizeof(T));
+    if (e != cudaSuccess) return e;
+    return cudaStreamSynchronize(cudaStreamLegacy);
 }
 
+// Device copy of a host vector, complete on return (a pageable cudaMemcpy may
+// return before its DMA has landed).
 template <typename T>
 cudaError_t upload(T** p, const std::vector<T>& v) {
     cudaError_t e = dalloc(p, (int64_t)v.size());
     if (e != cudaSuccess || v.empty()) return e;
-    return cudaMemcpy(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+    e = cudaMemcpy(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return e;
+    return cudaStreamSynchronize(cudaStreamLegacy);
 }
 
 void freeProblem(vfem_problem* p) {
@@ -286,6 +318,15 @@ vfem_status invertCoarseLarge(vfem_problem* p, T* K, int64_t n, cusolverDnHandle
              CUSOLVER_STATUS_SUCCESS))
         st = fail(VFEM_ERR_CUDA, "cusolver 64-bit buffer size query failed");
     std::vector<char> hws(std::max<size_t>(1, std::max(wh1, wh2)));
+    if (st == VFEM_OK) {
+        // the syrk result is a second n x n matrix: fail early, with the size, when it cannot fit
+        const size_t need = sizeof(T) * (size_t)(n * n) + std::max(wd1, wd2);
+        size_t freeB = 0, totalB = 0;
+        if (cudaMemGetInfo(&freeB, &totalB) == cudaSuccess && freeB < need)
+            st = fail(VFEM_ERR_OUT_OF_MEMORY, "coarse inverse of " + std::to_string(n) + " free DOFs needs " +
+                                                  std::to_string(need >> 20) + " MiB more device memory (" +
+                                                  std::to_string(freeB >> 20) + " MiB free)");
+    }
     if (st == VFEM_OK && (cudaMalloc(&dws, std::max<size_t>(16, std::max(wd1, wd2))) != cudaSuccess ||
                           cudaMalloc(&info, sizeof(int)) != cudaSuccess || dalloc(&C, n * n) != cudaSuccess))
         st = fail(VFEM_ERR_OUT_OF_MEMORY, "coarse inverse workspace");
@@ -342,7 +383,7 @@ vfem_status invertCoarse(vfem_problem* p, const float* E, double scale, T* K) {
     CK(cudaMemsetAsync(K, 0, sizeof(T) * (size_t)(n * n), p->stream));
     p->launches += launchAssembleCoarse<T>(p->stream, dc.g, E, p->dFreeNode, p->ke.Ke, scale, K, n);
     CK(cudaGetLastError());
-    if (n > kMaxCoarse32) {
+    if (n > g_coarse64Min) {
         cusolverDnHandle_t hl = nullptr;
         if (cusolverDnCreate(&hl) != CUSOLVER_STATUS_SUCCESS) return fail(VFEM_ERR_CUDA, "cusolverDnCreate failed");
         cusolverDnSetStream(hl, p->stream);
@@ -489,10 +530,11 @@ vfem_status buildHierarchyDevice(vfem_problem* p, const std::vector<LevelPlan>& 
     double* dtab = nullptr;
     int64_t* dfixed = nullptr;
     unsigned* dmax = nullptr;
+    int32_t* store = nullptr;  // a level's compressed numbering before it is trimmed
     vfem_status result = VFEM_OK;
     auto cleanup = [&]() {
         cudaFree(dcnt); cudaFree(scratch); cudaFree(dvox); cudaFree(dEin); cudaFree(dtab); cudaFree(dfixed);
-        cudaFree(dmax);
+        cudaFree(dmax); cudaFree(store);
     };
 #define CKS(call)                                                                                        \
     do {                                                                                                 \
@@ -532,7 +574,6 @@ vfem_status buildHierarchyDevice(vfem_problem* p, const std::vector<LevelPlan>& 
             CKS(gpuCoarseLevel(st, f.g, d.g, d.div, f.E, f.Ev, f.flags, d.E, d.Ev, d.flags, c));
         }
         // compressed numbering: sized by the node count, trimmed below
-        int32_t* store = nullptr;
         CKS(dalloc(&store, nn));
         CKS(gpuCompactUsed(st, d.g, d.flags, scratch, store, c));
         CKS(cudaMemcpyAsync(&hcnt[i], c, sizeof(SetupCounters), cudaMemcpyDeviceToHost, st));
@@ -547,7 +588,6 @@ vfem_status buildHierarchyDevice(vfem_problem* p, const std::vector<LevelPlan>& 
                     result = fail(VFEM_ERR_INVALID_ARGUMENT, "fixed node id out of range");
         }
         if (result != VFEM_OK) {
-            cudaFree(store);
             cleanup();
             return result;
         }
@@ -557,6 +597,7 @@ vfem_status buildHierarchyDevice(vfem_problem* p, const std::vector<LevelPlan>& 
         CKS(cudaMemcpyAsync(d.nodeStore, store, sizeof(int32_t) * (size_t)d.nused, cudaMemcpyDeviceToDevice, st));
         CKS(cudaStreamSynchronize(st));
         cudaFree(store);
+        store = nullptr;
         if (i == 0) {
             if (nfixed > 0) {
                 CKS(dalloc(&dfixed, nfixed));
@@ -606,6 +647,8 @@ vfem_status createImpl(const uint8_t* vox, int nx, int ny, int nz, const double*
         return fail(VFEM_ERR_INVALID_ARGUMENT, "null pointer argument");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(VFEM_ERR_NO_DEVICE, "no CUDA device");
+    g_coarse64Min = std::max<long long>(1, envInt("VFEM_COARSE_64BIT_MIN", kMaxCoarse32));
+    g_allocCountdown = std::max<long long>(0, envInt("VFEM_FAULT_ALLOC_AT", 0));
     vfem_problem* p = new vfem_problem();
     CK(cudaGetDevice(&p->device));
     vfem_status st = prepareKe(Ke, p->ke);
@@ -615,9 +658,9 @@ vfem_status createImpl(const uint8_t* vox, int nx, int ny, int nz, const double*
     }
     {
         // Reducing kernels keep one partial per block; the largest grids are the
-        // matvec tiles (31 x 7 x 16 owned nodes) and the 32 x 8 x 8-node per-node kernels.
+        // matvec tiles (31 x 7 x 32 owned nodes) and the 32 x 8 x 8-node per-node kernels.
         const int64_t gx = nx + 1, gy = ny + 1, gz = nz + 1;
-        const int64_t mv = ((gx + 30) / 31) * ((gy + 6) / 7) * ((gz + 15) / 16);
+        const int64_t mv = ((gx + 30) / 31) * ((gy + 6) / 7) * ((gz + 31) / 32);
         const int64_t pn = ((gx + 31) / 32) * ((gy + 7) / 8) * ((gz + 7) / 8);
         if (mv > kMaxRedBlocks || pn > kMaxRedBlocks) {
             delete p;
@@ -913,19 +956,16 @@ int iteration(vfem_problem* p, const vfem_options& o, double** zOut64, float** z
 vfem_status checkOptions(const vfem_options& o) {
     if (!(o.rtol > 0) || o.mg_mode < 0 || o.mg_mode > 2 || o.precision < 0 || o.precision > 1 ||
         (o.mg_mode == VFEM_MG_VCYCLE && (!(o.omega > 0) || o.pre_sweeps < 1 || o.post_sweeps < 0)) ||
-        o.check_every < 1 || o.check_every > 1024 || o.replace_every < 0 || !(o.replace_delta >= 0.0 && o.replace_delta < 1.0))
+        o.check_every < 1 || o.check_every > 1024 || o.replace_every < 0 ||
+        !(o.replace_delta >= 0.0 && o.replace_delta < 1.0) || o.fallback_fp64 < 0 || o.fallback_fp64 > 1 ||
+        o.debug_break_at < 0)
         return fail(VFEM_ERR_INVALID_ARGUMENT, "invalid solver options");
     return VFEM_OK;
 }
 
-vfem_status solveImpl(vfem_problem* p, const vfem_options* optIn, bool haveX0, vfem_stats* st) {
-    vfem_options o;
-    vfem_options_default(&o);
-    if (optIn) o = *optIn;
-    vfem_status s = checkOptions(o);
-    if (s != VFEM_OK) return s;
-    CK(cudaSetDevice(p->device));
-    s = o.precision == VFEM_PREC_FP64 ? ensureCoarse<double>(p, o.mg_mode == VFEM_MG_VCYCLE)
+// One solve with validated options o; x64 holds the initial guess when haveX0.
+vfem_status solvePhase(vfem_problem* p, const vfem_options& o, bool haveX0, vfem_stats* st) {
+    vfem_status s = o.precision == VFEM_PREC_FP64 ? ensureCoarse<double>(p, o.mg_mode == VFEM_MG_VCYCLE)
                                       : ensureCoarse<float>(p, o.mg_mode == VFEM_MG_VCYCLE);
     if (s != VFEM_OK) return s;
     DevLevel& l0 = p->L[0];
@@ -939,7 +979,7 @@ vfem_status solveImpl(vfem_problem* p, const vfem_options* optIn, bool haveX0, v
     CK(cudaEventCreate(&e1));
     CK(cudaEventRecord(e0, p->stream));
     launches += launchInitScalars(p->stream, p->S, o.rtol, maxIter, o.flexible, mixed ? 1 : 0,
-                                  mixed ? o.replace_every : 0, o.replace_delta);
+                                  mixed ? o.replace_every : 0, o.replace_delta, o.debug_break_at);
     // ---- initial residual, norms, first direction
     double* z64 = nullptr;
     float* z32 = nullptr;
@@ -1022,7 +1062,8 @@ vfem_status solveImpl(vfem_problem* p, const vfem_options* optIn, bool haveX0, v
     double relTrue = NAN;
     if (mixed && hs.done == CONVERGED && hs.replacements > 0 && hs.rhsNorm2 > 0) {
         relTrue = std::sqrt(hs.rrTrue / hs.rhsNorm2);
-    } else if (o.compute_true_residual && hs.rhsNorm2 > 0) {
+    } else if ((o.compute_true_residual || (mixed && hs.done != CONVERGED)) && hs.rhsNorm2 > 0) {
+        // (a failed mixed solve always reports it: the FP64 fallback starts from x when it is finite)
         MatvecArgs<double> a = mvArgs<double>(p, 0, p->x64, l0.t64, MV_RESID);
         a.f = p->f64;
         a.checkDone = 0;
@@ -1040,7 +1081,7 @@ vfem_status solveImpl(vfem_problem* p, const vfem_options* optIn, bool haveX0, v
     g_launches += launches;
     vfem_status result = VFEM_OK;
     if (hs.done == BREAKDOWN) result = VFEM_ERR_BREAKDOWN;
-    else if (hs.done == MAXITER || hs.done == RUNNING) result = VFEM_ERR_NOT_CONVERGED;
+    else if (hs.done == MAXITER || hs.done == RUNNING || hs.done == STAGNATED) result = VFEM_ERR_NOT_CONVERGED;
     if (st) {
         st->iterations = hs.iter;
         st->matvecs = hs.matvecs;
@@ -1052,8 +1093,50 @@ vfem_status solveImpl(vfem_problem* p, const vfem_options* optIn, bool haveX0, v
         st->status = result;
     }
     if (result == VFEM_ERR_BREAKDOWN) g_lastError = "PCG breakdown (p^T A p <= 0 or non-finite scalar)";
-    if (result == VFEM_ERR_NOT_CONVERGED) g_lastError = "maximum iterations reached";
+    if (result == VFEM_ERR_NOT_CONVERGED)
+        g_lastError = hs.done == STAGNATED ? "mixed-precision true residual stagnated" : "maximum iterations reached";
     return result;
+}
+
+// The solve with its FP64 fallback: a mixed-precision solve that breaks down or
+// stops short of rtol hands its iterate to plain FP64 MG-PCG (the reference's
+// method), which gets the iterations left of the budget.
+vfem_status solveImpl(vfem_problem* p, const vfem_options* optIn, bool haveX0, vfem_stats* st) {
+    vfem_options o;
+    vfem_options_default(&o);
+    if (optIn) o = *optIn;
+    vfem_status s = checkOptions(o);
+    if (s != VFEM_OK) return s;
+    CK(cudaSetDevice(p->device));
+    vfem_stats s1;
+    std::memset(&s1, 0, sizeof(s1));
+    s = solvePhase(p, o, haveX0, &s1);
+    const long long budget = o.max_iter > 0 ? o.max_iter : 2 * 3 * p->L[0].nused;
+    const bool retry = o.precision == VFEM_PREC_MIXED && o.fallback_fp64 &&
+                       (s == VFEM_ERR_BREAKDOWN || s == VFEM_ERR_NOT_CONVERGED) && s1.iterations < budget;
+    if (!retry) {
+        if (st) *st = s1;
+        return s;
+    }
+    vfem_options o2 = o;
+    o2.precision = VFEM_PREC_FP64;
+    o2.max_iter = budget - s1.iterations;
+    o2.debug_break_at = 0;
+    vfem_stats s2;
+    std::memset(&s2, 0, sizeof(s2));
+    s = solvePhase(p, o2, std::isfinite(s1.rel_residual), &s2);
+    if (st) {
+        *st = s2;
+        st->iterations = s1.iterations + s2.iterations;
+        st->matvecs = s1.matvecs + s2.matvecs;
+        st->residual_replacements = s1.residual_replacements;
+        st->solve_ms = s1.solve_ms + s2.solve_ms;
+        st->kernel_launches = s1.kernel_launches + s2.kernel_launches;
+        st->fallback = 1;
+        st->fallback_iterations = s2.iterations;
+        st->status = s;
+    }
+    return s;
 }
 
 // Host compressed vector -> dense device vector of level lv.  checkFinite: the
@@ -1124,6 +1207,8 @@ void vfem_options_default(vfem_options* o) {
     o->check_every = 8;
     o->compute_true_residual = 1;
     o->replace_delta = 0.05;
+    o->fallback_fp64 = 1;
+    o->debug_break_at = 0;
 }
 
 const char* vfem_status_string(vfem_status s) {
@@ -1157,7 +1242,10 @@ vfem_status vfem_problem_create(const uint8_t* voxels, int32_t nx, int32_t ny, i
                                 const float* E_or_null, const int64_t* fixed_nodes, int64_t nfixed,
                                 int32_t num_levels, int32_t skip_levels, vfem_problem** out) {
     if (out) *out = nullptr;
-    return createImpl(voxels, nx, ny, nz, Ke, E_or_null, fixed_nodes, nfixed, num_levels, skip_levels, out);
+    const vfem_status s =
+        createImpl(voxels, nx, ny, nz, Ke, E_or_null, fixed_nodes, nfixed, num_levels, skip_levels, out);
+    g_allocCountdown = 0;  // the allocation-failure hook covers one set-up only
+    return s;
 }
 
 void vfem_problem_destroy(vfem_problem* p) { freeProblem(p); }
@@ -1249,7 +1337,8 @@ vfem_status vfem_apply_operator_device_noalloc(vfem_problem* p, const double* x_
     CK(launchMatvecNoAlloc(static_cast<cudaStream_t>(stream), a, p->ke.structured, p->op64, xKx_device, &tooLarge));
     if (tooLarge)
         return fail(VFEM_ERR_INVALID_ARGUMENT,
-                    "grid too large for the no-allocation scratch (at most 65536 product blocks of 31x7x16 nodes)");
+                    "grid too large for the no-allocation scratch (at most 65536 product blocks of 31x7x32 "
+                    "nodes, about 760^3 nodes for a cube)");
     p->launches += 1;
     g_launches += 1;
     return VFEM_OK;

@@ -98,6 +98,7 @@ __device__ void applyEpi(int epi, Scalars* S, double t0, double t1) {
             S->red1 = t1;
             break;
         case EPI_ALPHA:
+            if (S->breakAt > 0 && S->iter + 1 >= S->breakAt) t0 = -1.0;  // forced breakdown (testing)
             S->pAp = t0;
             S->matvecs++;
             if (!(t0 > 0.0) || !isfinite(t0)) S->done = BREAKDOWN;
@@ -133,6 +134,9 @@ __device__ void applyEpi(int epi, Scalars* S, double t0, double t1) {
             if (t0 == 0.0 || t1 < S->threshold) S->done = CONVERGED;
             break;
         case EPI_TRUE:
+            if (S->replacements > 0 && t0 >= 0.98 * S->rrTruePrev) S->stalls++;
+            else S->stalls = 0;
+            S->rrTruePrev = t0;
             S->replStamp = S->matvecs;
             S->rrTrue = t0;
             S->rr = t0;
@@ -141,6 +145,7 @@ __device__ void applyEpi(int epi, Scalars* S, double t0, double t1) {
             S->replacements++;
             if (!isfinite(t0)) S->done = BREAKDOWN;
             else if (t0 < S->threshold) S->done = CONVERGED;
+            else if (S->stalls >= 3) S->done = STAGNATED;
             break;
         default:
             break;
@@ -350,11 +355,16 @@ __device__ __forceinline__ void ldSlot<double>(const double* p, double& a, doubl
 }
 
 // Output stage of the matvec kernels for one owned node s: sum = (K x)_s before
-// the fixed-row mask; writes y (and y32) by mode and accumulates the dots.
+// the fixed-row mask; writes y (and y32) by mode and accumulates the dots.  fl:
+// the node's flags.  The x.(Kx) term skips unused and fixed nodes, where Kx is
+// 0, so that whatever x holds there (the caller's buffer may carry NaN at nodes
+// no element touches) cannot reach the dot.
 template <typename T, typename TC>
-__device__ __forceinline__ void mvOutput(const MatvecArgs<T>& a, int64_t s, const TC (&sum)[3], bool fixed,
+__device__ __forceinline__ void mvOutput(const MatvecArgs<T>& a, int64_t s, const TC (&sum)[3], uint8_t fl,
                                          const TC (&xo)[3], DotAcc<TC>& d0, DotAcc<TC>& d1) {
     typedef Cvt<T, TC> C;
+    const bool fixed = (fl & FLAG_FIXED) != 0;
+    const bool live = (fl & FLAG_USED) && !fixed;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
         const TC ax = fixed ? TC(0) : sum[c];
@@ -371,7 +381,7 @@ __device__ __forceinline__ void mvOutput(const MatvecArgs<T>& a, int64_t s, cons
         if constexpr (std::is_same<T, TC>::value) a.y[3 * s + c] = out;
         else if (a.y) a.y[3 * s + c] = C::out(out);
         if (a.y32) a.y32[3 * s + c] = toF(out);
-        if (a.dot0 == DOT_X_OUT) d0.add(xv * out);
+        if (a.dot0 == DOT_X_OUT) d0.add(live ? xv * out : TC(0));
         else if (a.dot0 == DOT_OUT_OUT) d0.add(out * out);
         else if (a.dot0 == DOT_F_OUT) d0.add(fv * out);
         if (a.dot1) d1.add(out * C::in(a.aux[3 * s + c]));
@@ -525,7 +535,7 @@ __global__ void __launch_bounds__(MV_TX* MV_TY, 1)
                 TC sum[3];
 #pragma unroll
                 for (int c = 0; c < 3; ++c) sum[c] = acc[c] + lo[c];
-                mvOutput<T, TC>(a, (int64_t)oCol + (int64_t)k * plane, sum, (fl & FLAG_FIXED) != 0, xo, d0, d1);
+                mvOutput<T, TC>(a, (int64_t)oCol + (int64_t)k * plane, sum, fl, xo, d0, d1);
             }
 #pragma unroll
             for (int c = 0; c < 3; ++c) acc[c] = hi[c];
@@ -808,7 +818,7 @@ __global__ void __launch_bounds__(MV_TX* MV_TY, sizeof(TC) == 4 ? 3 : 2)
                     d0.add(out * out);
                 }
             } else {
-                mvOutput<T, TC>(a, s, sum, (fl & FLAG_FIXED) != 0, xo, d0, d1);
+                mvOutput<T, TC>(a, s, sum, fl, xo, d0, d1);
             }
         }
     }
@@ -1797,8 +1807,9 @@ __global__ void kSymmetrize(T* K, int64_t n) {
 }
 
 __global__ void kInitScalars(Scalars* S, double tol, long long maxIter, int flexible, int mixed, int replaceEvery,
-                             double delta) {
+                             double delta, int breakAt) {
     Scalars s = {};
+    s.breakAt = breakAt;
     s.tol2 = tol * tol;
     s.maxIter = maxIter;
     s.flexible = flexible;
@@ -2090,8 +2101,8 @@ int launchSymmetrizeLowerToFull(cudaStream_t s, T* K, int64_t n) {
 }
 
 int launchInitScalars(cudaStream_t s, Scalars* S, double tol, long long maxIter, int flexible, int mixed,
-                      int replaceEvery, double replaceDelta) {
-    kInitScalars<<<1, 1, 0, s>>>(S, tol, maxIter, flexible, mixed, replaceEvery, replaceDelta);
+                      int replaceEvery, double replaceDelta, int breakAt) {
+    kInitScalars<<<1, 1, 0, s>>>(S, tol, maxIter, flexible, mixed, replaceEvery, replaceDelta, breakAt);
     return 1;
 }
 
@@ -2136,7 +2147,7 @@ cudaError_t launchMatvecNoAlloc(cudaStream_t s, const MatvecArgs<double>& a, boo
     cudaError_t e = noallocScratchSetup();
     if (e != cudaSuccess) return e;
     int dev = 0;
-    cudaGetDevice(&dev);
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
     unsigned char* base = static_cast<unsigned char*>(g_noallocAddr[dev]);
     RedBuf rb{reinterpret_cast<double*>(base), reinterpret_cast<unsigned*>(base + kNoAllocPartialBytes)};
     Scalars* S = reinterpret_cast<Scalars*>(base + kNoAllocPartialBytes + 256);

@@ -14,7 +14,9 @@
 
 namespace vfem {
 
-enum Done : int { RUNNING = 0, CONVERGED = 1, MAXITER = 2, BREAKDOWN = 3 };
+// STAGNATED (mixed precision): three replacements in a row found the true
+// residual no more than 1% below the previous one.
+enum Done : int { RUNNING = 0, CONVERGED = 1, MAXITER = 2, BREAKDOWN = 3, STAGNATED = 4 };
 
 struct Scalars {
     double rhsNorm2, threshold, tol2;
@@ -28,11 +30,13 @@ struct Scalars {
     int flexible;
     int mixed;
     int replaceEvery;
-    int pad;
+    int breakAt;       // testing: pAp of this iteration (1-based) is taken as -1 (0 = off)
     // mixed precision, deferred x += alpha p: value of `matvecs` when the
     // residual update last ran, when a conditional kFlushX folded alpha p, when
     // kUpdatePX ran; replStamp: when the true residual last replaced r
     long long rStamp, foldStamp, pxStamp, replStamp;
+    double rrTruePrev;  // true r.r of the previous replacement
+    long long stalls;   // consecutive replacements without a 1% drop of the true residual
 };
 
 struct RedBuf {
@@ -211,7 +215,7 @@ int launchZeroStrictRowMajorLower(cudaStream_t s, T* K, int64_t n);
 
 // Solver scalar initialisation (device side, so it can live in a graph).
 int launchInitScalars(cudaStream_t s, Scalars* S, double tol, long long maxIter, int flexible, int mixed,
-                      int replaceEvery, double replaceDelta);
+                      int replaceEvery, double replaceDelta, int breakAt = 0);
 
 // FP64 product y = K x with the fused x.(Kx) dot, its reduction scratch taken from
 // a file-scope device array (kernels.cu) instead of allocated memory.  The first

@@ -429,11 +429,15 @@ vfem_status netFail(vfem_status s, const std::string& m) {
         if (e_ != cudaSuccess) return netFail(VFEM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
     } while (0)
 
+// Zeroed device allocation, complete on return (the memset runs on the legacy
+// default stream, which the network's non-blocking stream does not wait for).
 template <typename T>
 cudaError_t nalloc(T** p, int64_t n) {
     cudaError_t e = cudaMalloc((void**)p, sizeof(T) * (size_t)(n > 0 ? n : 1));
     if (e != cudaSuccess) return e;
-    return cudaMemset(*p, 0, sizeof(T) * (size_t)(n > 0 ? n : 1));
+    e = cudaMemset(*p, 0, sizeof(T) * (size_t)(n > 0 ? n : 1));
+    if (e != cudaSuccess) return e;
+    return cudaStreamSynchronize(cudaStreamLegacy);
 }
 
 void conv(vfem_net* N, const bf16* in, const bf16* W, const float* b, void* out, int lvl, int Cin, int Cout, int relu,
