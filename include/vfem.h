@@ -161,6 +161,19 @@ vfem_status vfem_solve_device(vfem_problem* p, const vfem_options* opt, double* 
  * fixed rows zeroed. */
 vfem_status vfem_apply_operator(vfem_problem* p, const double* x, double* y);
 
+/* The same product as the mixed-precision solver applies it (no counterpart in
+ * the reference): x rounded to FP32, y = K x with the fixed rows zeroed computed
+ * in FP32 (on the tensor cores when vfem_problem_uses_tensor_cores is 1, else on
+ * the CUDA cores), returned in FP64; xKx_or_null receives x.(Kx) summed in FP64. */
+vfem_status vfem_apply_operator_mixed(vfem_problem* p, const double* x, double* y, double* xKx_or_null);
+
+/* 1 when the mixed-precision solver's CG product runs on the tensor cores.  It
+ * does when the environment variable VFEM_TENSOR_CORE_PRODUCT was set to a
+ * non-zero value when the problem was created and Ke times some integer
+ * q <= 65536 is integer-valued and exact in BF16 (q = 1872 for the 2x2x2-Gauss
+ * hex at nu = 0.3).  Off by default: on GB300 the CUDA-core product is faster. */
+int32_t vfem_problem_uses_tensor_cores(const vfem_problem* p);
+
 /* No counterpart in the reference.  The operator product of vfem_apply_operator
  * for callers that cannot allocate GPU memory at the point of the call: hosts
  * that hand every byte of device memory to their own pool up front (a solver
@@ -225,7 +238,8 @@ typedef enum vfem_kernel_class {
     VFEM_K_COARSE_FP32 = 11,
     VFEM_K_TRUE_RESIDUAL_DF = 12, /* f - K x on FP64 vectors in double-float arithmetic */
     VFEM_K_UPDATE_RESTRICT_MIXED = 13, /* mixed: r -= alpha Ap, r.r and the first restriction in one pass */
-    VFEM_K_COUNT = 14
+    VFEM_K_MATVEC_FP32_SIMT = 14, /* the FP32 CG product on the CUDA cores, whichever product the problem uses */
+    VFEM_K_COUNT = 15
 } vfem_kernel_class;
 
 /* Measurement helper (no counterpart in the reference): average device time in

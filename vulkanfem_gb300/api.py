@@ -43,7 +43,7 @@ EXPORTED = (
     "vfem_apply_preconditioner_mixed",
     "vfem_restrict", "vfem_interpolate", "vfem_inverse_diagonal", "vfem_fixed_nodes",
     "vfem_kernel_launch_count", "vfem_last_error_message", "vfem_profile_kernels",
-    "vfem_apply_operator_device_noalloc",
+    "vfem_apply_operator_device_noalloc", "vfem_apply_operator_mixed", "vfem_problem_uses_tensor_cores",
     # learned warm start (include/vfem_net.h)
     "vfem_net_create", "vfem_net_destroy", "vfem_net_num_params", "vfem_net_set_params", "vfem_net_get_params",
     "vfem_net_forward", "vfem_net_train_batch", "vfem_net_last_error_message",
@@ -51,7 +51,7 @@ EXPORTED = (
 
 KERNEL_CLASSES = ("matvec_fp64", "matvec_fp32", "restrict_fp64", "restrict_fp32", "prolong_fp64", "prolong_fp32",
                   "update_xr_fp64", "update_xr_mixed", "update_p_fp64", "update_p_fp32", "coarse_fp64",
-                  "coarse_fp32", "true_residual_df", "update_restrict_mixed")
+                  "coarse_fp32", "true_residual_df", "update_restrict_mixed", "matvec_fp32_simt")
 
 
 class VfemError(RuntimeError):
@@ -132,6 +132,9 @@ def load_library(build_if_missing=True):
     lib.vfem_profile_kernels.argtypes = [P, i32, f64p]
     lib.vfem_apply_operator_device_noalloc.argtypes = [P, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                                        ctypes.c_void_p]
+    lib.vfem_apply_operator_mixed.argtypes = [P, f64p, f64p, ctypes.c_void_p]
+    lib.vfem_problem_uses_tensor_cores.argtypes = [P]
+    lib.vfem_problem_uses_tensor_cores.restype = ctypes.c_int32
     for name in EXPORTED:
         fn = getattr(lib, name)
         if fn.restype is ctypes.c_int and name not in ("vfem_status_string",):
@@ -260,6 +263,21 @@ class MatrixFreeSparse:
         return y
 
     __matmul__ = dot
+
+    def dot_mixed(self, x):
+        """The mixed-precision solver's product: FP32 (tensor cores when
+        ``uses_tensor_cores``).  Returns (K x, x.(Kx))."""
+        x = np.ascontiguousarray(x, np.float64)
+        if x.size != self.rows():
+            raise VfemError(1, "vector size mismatch")
+        y = np.empty_like(x)
+        d = ctypes.c_double()
+        _check(self._lib.vfem_apply_operator_mixed(self._h, x, y, ctypes.cast(ctypes.pointer(d), ctypes.c_void_p)))
+        return y, d.value
+
+    @property
+    def uses_tensor_cores(self):
+        return bool(self._lib.vfem_problem_uses_tensor_cores(self._h))
 
     def restrict(self, level, v):
         v = np.ascontiguousarray(v, np.float64)

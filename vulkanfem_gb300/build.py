@@ -16,7 +16,7 @@ LIB = os.path.join(BUILD, "libvfem.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["setup.cpp", "setup_gpu.cu", "kernels.cu", "api.cu", "unet.cu"]
+SOURCES = ["setup.cpp", "setup_gpu.cu", "kernels.cu", "matvec_tc.cu", "api.cu", "unet.cu"]
 
 
 def nvcc():
@@ -34,7 +34,7 @@ def _stale(out, deps):
 
 
 def _headers():
-    hs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".h")]
+    hs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     hs += [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith(".h")]
     return hs
 

@@ -141,6 +141,9 @@ struct vfem_problem {
     // constants for the kernels
     double op64[45 + 576];
     float op32[45 + 576];
+    // the tensor-core FP32 CG product (matvec_tc.cu), opt-in, when Ke admits an exact BF16 scaling
+    TcOperand tc;
+    bool tcReady = false;
     std::map<GraphKey, CachedGraph> graphs;
     bool rhsSet = false;
     long long launches = 0;
@@ -697,6 +700,10 @@ vfem_status createImpl(const uint8_t* vox, int nx, int ny, int nz, const double*
     } while (0)
     CKP(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking));
     CKP(setKernelAttributes());
+    // VFEM_TENSOR_CORE_PRODUCT=1: the FP32 CG product on the tensor cores (slower
+    // than the CUDA-core kernel on GB300; kept as a measured alternative)
+    p->tcReady = envInt("VFEM_TENSOR_CORE_PRODUCT", 0) != 0 && tcPrepare(p->ke.Ke, p->tc) &&
+                 tcBlocks(plan[0].g) <= kMaxRedBlocks && tcSetAttributes() == cudaSuccess;
     st = buildHierarchyDevice(p, plan, vox, E, fixed, nfixed);
     if (st != VFEM_OK) return bail(st);
     for (DevLevel& d : p->L) {
@@ -794,8 +801,14 @@ MatvecArgs<T> mvArgs(vfem_problem* p, int lv, const T* x, T* y, int mode) {
     return a;
 }
 
+// FP32 CG products (y = K x, fixed rows 0, x.(Kx)) run on the tensor cores when
+// the problem was created with them enabled; every other product runs on the
+// CUDA-core kernels.
 template <typename T>
-int matvec(vfem_problem* p, const MatvecArgs<T>& a) {
+int matvec(vfem_problem* p, const MatvecArgs<T>& a, bool allowTc = true) {
+    if constexpr (std::is_same<T, float>::value) {
+        if (allowTc && p->tcReady && tcEligible(a)) return launchMatvecTC(ctx(p), a, p->tc);
+    }
     return launchMatvec<T>(ctx(p), a, p->ke.structured, opc<T>(p));
 }
 
@@ -1080,7 +1093,8 @@ vfem_status solvePhase(vfem_problem* p, const vfem_options& o, bool haveX0, vfem
     p->launches += launches;
     g_launches += launches;
     vfem_status result = VFEM_OK;
-    if (hs.done == BREAKDOWN) result = VFEM_ERR_BREAKDOWN;
+    if (hs.kernelTimeout) result = VFEM_ERR_TIMEOUT;
+    else if (hs.done == BREAKDOWN) result = VFEM_ERR_BREAKDOWN;
     else if (hs.done == MAXITER || hs.done == RUNNING || hs.done == STAGNATED) result = VFEM_ERR_NOT_CONVERGED;
     if (st) {
         st->iterations = hs.iter;
@@ -1092,6 +1106,7 @@ vfem_status solvePhase(vfem_problem* p, const vfem_options& o, bool haveX0, vfem
         st->kernel_launches = launches;
         st->status = result;
     }
+    if (result == VFEM_ERR_TIMEOUT) g_lastError = "a kernel's bounded wait ran out (tensor-core product)";
     if (result == VFEM_ERR_BREAKDOWN) g_lastError = "PCG breakdown (p^T A p <= 0 or non-finite scalar)";
     if (result == VFEM_ERR_NOT_CONVERGED)
         g_lastError = hs.done == STAGNATED ? "mixed-precision true residual stagnated" : "maximum iterations reached";
@@ -1328,6 +1343,34 @@ vfem_status vfem_apply_operator(vfem_problem* p, const double* x, double* y) {
     return fromDenseHost(p, 0, p->Ap64, y);
 }
 
+vfem_status vfem_apply_operator_mixed(vfem_problem* p, const double* x, double* y, double* xKx) {
+    if (!p || !x || !y) return fail(VFEM_ERR_INVALID_ARGUMENT, "null argument");
+    CK(cudaSetDevice(p->device));
+    DevLevel& l0 = p->L[0];
+    const int64_t n = l0.nvec();
+    vfem_status s = toDenseHost(p, 0, x, p->p64, false);
+    if (s != VFEM_OK) return s;
+    int k = launchConvert<double, float>(p->stream, n, p->p64, p->p32);
+    k += launchInitScalars(p->stream, p->S, 1e-6, 1, 0, 1, 0, 0.0);
+    MatvecArgs<float> a = mvArgs<float>(p, 0, p->p32, p->Ap32, MV_AX);
+    a.checkDone = 0;
+    a.dot0 = DOT_X_OUT;
+    a.epi = EPI_STORE;
+    k += matvec<float>(p, a);
+    k += launchConvert<float, double>(p->stream, n, p->Ap32, p->Ap64);
+    p->launches += k;
+    g_launches += k;
+    CK(cudaGetLastError());
+    s = fromDenseHost(p, 0, p->Ap64, y);  // synchronises the stream
+    if (s != VFEM_OK) return s;
+    CK(cudaMemcpy(p->hS, p->S, sizeof(Scalars), cudaMemcpyDeviceToHost));
+    if (p->hS->kernelTimeout) return fail(VFEM_ERR_TIMEOUT, "a kernel's bounded wait ran out (tensor-core product)");
+    if (xKx) *xKx = p->hS->red0;
+    return VFEM_OK;
+}
+
+int32_t vfem_problem_uses_tensor_cores(const vfem_problem* p) { return p && p->tcReady ? 1 : 0; }
+
 vfem_status vfem_apply_operator_device_noalloc(vfem_problem* p, const double* x_device, double* y_device,
                                                double* xKx_device, void* stream) {
     if (!p || !x_device || !y_device || !xKx_device) return fail(VFEM_ERR_INVALID_ARGUMENT, "null argument");
@@ -1452,11 +1495,12 @@ vfem_status vfem_profile_kernels(vfem_problem* p, int32_t reps, double* ms) {
                     a.epi = EPI_STORE;
                     return matvec<double>(p, a);
                 }
-                case VFEM_K_MATVEC_FP32: {
+                case VFEM_K_MATVEC_FP32:
+                case VFEM_K_MATVEC_FP32_SIMT: {
                     MatvecArgs<float> a = mvArgs<float>(p, 0, p->p32, p->Ap32, MV_AX);
                     a.dot0 = DOT_X_OUT;
                     a.epi = EPI_STORE;
-                    return matvec<float>(p, a);
+                    return matvec<float>(p, a, k == VFEM_K_MATVEC_FP32);
                 }
                 case VFEM_K_RESTRICT_FP64:
                     return two ? launchRestrict<double>(c, l0.g, l1.g, l1.div, l0.r64, l1.r64, 1) : 0;

@@ -37,6 +37,8 @@ struct Scalars {
     long long rStamp, foldStamp, pxStamp, replStamp;
     double rrTruePrev;  // true r.r of the previous replacement
     long long stalls;   // consecutive replacements without a 1% drop of the true residual
+    int kernelTimeout;  // a kernel's bounded wait ran out (the solve stops with BREAKDOWN)
+    int pad2;
 };
 
 struct RedBuf {
@@ -224,6 +226,21 @@ int launchInitScalars(cudaStream_t s, Scalars* S, double tol, long long maxIter,
 // the array holds.  xKx is a device pointer.
 cudaError_t launchMatvecNoAlloc(cudaStream_t s, const MatvecArgs<double>& a, bool structured, const void* opconst,
                                 double* xKx, bool* tooLarge);
+
+// Tensor-core FP32 CG product (matvec_tc.cu): B = q Ke in BF16 as K-major core
+// matrices, invScale = 1 / q.  tcPrepare fails (false) when no integer
+// q <= 65536 makes every entry of q Ke an integer exact in BF16.
+struct alignas(16) TcOperand {
+    uint32_t b[512];
+    float invScale;
+    int q;
+};
+bool tcPrepare(const double* Ke, TcOperand& out);
+// The product form the tensor-core kernel computes: y = K x (fixed rows 0) and x.(Kx).
+bool tcEligible(const MatvecArgs<float>& a);
+cudaError_t tcSetAttributes();
+int launchMatvecTC(const LaunchCtx& c, const MatvecArgs<float>& a, const TcOperand& op);
+int64_t tcBlocks(const Grid& g);  // reduction blocks of a launch
 
 // Device-side ``done`` / iteration snapshot is read back by the host with a plain copy.
 
