@@ -174,6 +174,13 @@ vfem_status vfem_apply_operator_mixed(vfem_problem* p, const double* x, double* 
  * hex at nu = 0.3).  Off by default: on GB300 the CUDA-core product is faster. */
 int32_t vfem_problem_uses_tensor_cores(const vfem_problem* p);
 
+/* Which staged transfer kernels the problem's mixed-precision V-cycle uses, as
+ * bits: 1 = the FP32 2x restrictions stage their fine rows with TMA tensor
+ * loads, 2 = the 2x up-leg stages its ranges with bulk copies.  Set from the
+ * environment variable VFEM_TMA_MASK when the problem is created; default 0:
+ * on GB300 both measured slower than the kernels that load directly. */
+int32_t vfem_problem_uses_tma(const vfem_problem* p);
+
 /* No counterpart in the reference.  The operator product of vfem_apply_operator
  * for callers that cannot allocate GPU memory at the point of the call: hosts
  * that hand every byte of device memory to their own pool up front (a solver

@@ -44,6 +44,7 @@ EXPORTED = (
     "vfem_restrict", "vfem_interpolate", "vfem_inverse_diagonal", "vfem_fixed_nodes",
     "vfem_kernel_launch_count", "vfem_last_error_message", "vfem_profile_kernels",
     "vfem_apply_operator_device_noalloc", "vfem_apply_operator_mixed", "vfem_problem_uses_tensor_cores",
+    "vfem_problem_uses_tma",
     # learned warm start (include/vfem_net.h)
     "vfem_net_create", "vfem_net_destroy", "vfem_net_num_params", "vfem_net_set_params", "vfem_net_get_params",
     "vfem_net_forward", "vfem_net_train_batch", "vfem_net_last_error_message",
@@ -135,6 +136,8 @@ def load_library(build_if_missing=True):
     lib.vfem_apply_operator_mixed.argtypes = [P, f64p, f64p, ctypes.c_void_p]
     lib.vfem_problem_uses_tensor_cores.argtypes = [P]
     lib.vfem_problem_uses_tensor_cores.restype = ctypes.c_int32
+    lib.vfem_problem_uses_tma.argtypes = [P]
+    lib.vfem_problem_uses_tma.restype = ctypes.c_int32
     for name in EXPORTED:
         fn = getattr(lib, name)
         if fn.restype is ctypes.c_int and name not in ("vfem_status_string",):
@@ -278,6 +281,10 @@ class MatrixFreeSparse:
     @property
     def uses_tensor_cores(self):
         return bool(self._lib.vfem_problem_uses_tensor_cores(self._h))
+
+    @property
+    def uses_tma(self):
+        return bool(self._lib.vfem_problem_uses_tma(self._h))
 
     def restrict(self, level, v):
         v = np.ascontiguousarray(v, np.float64)

@@ -16,7 +16,7 @@ LIB = os.path.join(BUILD, "libvfem.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["setup.cpp", "setup_gpu.cu", "kernels.cu", "matvec_tc.cu", "api.cu", "unet.cu"]
+SOURCES = ["setup.cpp", "setup_gpu.cu", "kernels.cu", "matvec_tc.cu", "transfer_tma.cu", "api.cu", "unet.cu"]
 
 
 def nvcc():

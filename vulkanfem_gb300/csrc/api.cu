@@ -144,6 +144,7 @@ struct vfem_problem {
     // the tensor-core FP32 CG product (matvec_tc.cu), opt-in, when Ke admits an exact BF16 scaling
     TcOperand tc;
     bool tcReady = false;
+    int tma = 0;  // bit 0: TMA-staged FP32 restrictions, bit 1: bulk-staged mixed prolongation (LaunchCtx::tma)
     std::map<GraphKey, CachedGraph> graphs;
     bool rhsSet = false;
     long long launches = 0;
@@ -172,9 +173,11 @@ vfem_status fail(vfem_status s, const std::string& msg) {
 template <typename T>
 cudaError_t dalloc(T** p, int64_t n) {
     if (g_allocCountdown > 0 && --g_allocCountdown == 0) return cudaErrorMemoryAllocation;  // testing hook
-    cudaError_t e = cudaMalloc((void**)p, (size_t)std::max<int64_t>(n, 1) * sizeof(T));
+    // 64 spare zero bytes: bulk copies widen their ranges to 16-byte boundaries
+    const size_t bytes = (size_t)std::max<int64_t>(n, 1) * sizeof(T) + 64;
+    cudaError_t e = cudaMalloc((void**)p, bytes);
     if (e != cudaSuccess) return e;
-    e = cudaMemset(*p, 0, (size_t)std::max<int64_t>(n, 1) * sizeof(T));
+    e = cudaMemset(*p, 0, bytes);
     if (e != cudaSuccess) return e;
     return cudaStreamSynchronize(cudaStreamLegacy);
 }
@@ -214,7 +217,7 @@ void freeProblem(vfem_problem* p) {
     delete p;
 }
 
-LaunchCtx ctx(vfem_problem* p) { return LaunchCtx{p->stream, p->S, p->rb}; }
+LaunchCtx ctx(vfem_problem* p) { return LaunchCtx{p->stream, p->S, p->rb, p->tma}; }
 
 template <typename T>
 vfem_status invertCoarse(vfem_problem* p, const float* E, double scale, T* K);
@@ -704,6 +707,9 @@ vfem_status createImpl(const uint8_t* vox, int nx, int ny, int nz, const double*
     // than the CUDA-core kernel on GB300; kept as a measured alternative)
     p->tcReady = envInt("VFEM_TENSOR_CORE_PRODUCT", 0) != 0 && tcPrepare(p->ke.Ke, p->tc) &&
                  tcBlocks(plan[0].g) <= kMaxRedBlocks && tcSetAttributes() == cudaSuccess;
+    // VFEM_TMA_MASK (default 0): bit 0 the FP32 restrictions with TMA-staged rows, bit 1 the
+    // mixed up-leg with bulk-staged ranges; both measured slower than the direct-load kernels
+    p->tma = tmaSetAttributes() == cudaSuccess ? (int)envInt("VFEM_TMA_MASK", 0) & 3 : 0;
     st = buildHierarchyDevice(p, plan, vox, E, fixed, nfixed);
     if (st != VFEM_OK) return bail(st);
     for (DevLevel& d : p->L) {
@@ -714,6 +720,7 @@ vfem_status createImpl(const uint8_t* vox, int nx, int ny, int nz, const double*
     int64_t nv0 = p->L[0].nvec();
     CKP(dalloc(&p->f64, nv0)); CKP(dalloc(&p->x64, nv0)); CKP(dalloc(&p->p64, nv0)); CKP(dalloc(&p->Ap64, nv0));
     CKP(dalloc(&p->p32, nv0)); CKP(dalloc(&p->Ap32, nv0)); CKP(dalloc(&p->x32, nv0)); CKP(dalloc(&p->r32b, nv0));
+    if (!tmaAvailable(p->r32b, nv0)) p->tma &= ~1;
     CKP(dalloc(&p->S, 1));
     CKP(dalloc(&p->rb.partials, 2 * (int64_t)kMaxRedBlocks));
     CKP(dalloc(&p->rb.ticket, 1));
@@ -1370,6 +1377,8 @@ vfem_status vfem_apply_operator_mixed(vfem_problem* p, const double* x, double* 
 }
 
 int32_t vfem_problem_uses_tensor_cores(const vfem_problem* p) { return p && p->tcReady ? 1 : 0; }
+
+int32_t vfem_problem_uses_tma(const vfem_problem* p) { return p ? p->tma : 0; }
 
 vfem_status vfem_apply_operator_device_noalloc(vfem_problem* p, const double* x_device, double* y_device,
                                                double* xKx_device, void* stream) {

@@ -36,31 +36,6 @@ constexpr int MV_TX = 32, MV_TY = 8, MV_ZC = 32;  // z layers per product block 
 constexpr int NT = 256;
 constexpr int PZ = 8;  // z nodes per thread in the per-node kernels
 
-// Per-thread dot-product accumulator.  FP64 vectors accumulate in FP64.  FP32
-// vectors accumulate in FP32 with Kahan compensation and are converted to FP64
-// once per thread, before the FP64 block and grid reduction: on GB300 the FP64
-// pipe is ~1/64 of FP32, so per-element FP64 conversions and FMAs would bound
-// the FP32 kernels.
-template <typename T>
-struct DotAcc;
-template <>
-struct DotAcc<double> {
-    double s = 0.0;
-    __device__ __forceinline__ void add(double v) { s += v; }
-    __device__ __forceinline__ double get() const { return s; }
-};
-template <>
-struct DotAcc<float> {
-    float s = 0.f, c = 0.f;
-    __device__ __forceinline__ void add(float v) {
-        const float y = v - c;
-        const float t = s + y;
-        c = (t - s) - y;
-        s = t;
-    }
-    __device__ __forceinline__ double get() const { return (double)s - (double)c; }
-};
-
 // Double-float ("df") numbers: the unevaluated sum hi + lo of two FP32 values,
 // about 48 significant bits, computed with FP32 instructions only (Dekker 1971:
 // TwoSum / FastTwoSum; the product error from one FMA).  GB300 issues FP64 at
@@ -1774,6 +1749,9 @@ int launchRestrict(const LaunchCtx& c, const Grid& gf, const Grid& gc, int div, 
     if (div == 4) {
         kRestrict<T, 4><<<nodeGrid(gc), block, 0, c.stream>>>(gf, gc, rf, rc, c.S, checkDone);
     } else {
+        if constexpr (std::is_same<T, float>::value) {
+            if ((c.tma & 1) && launchRestrictTma(c, gf, gc, rf, nullptr, nullptr, rc, checkDone)) return 1;
+        }
         dim3 grid((gc.nx + 31) / 32, (gc.ny + 7) / 8, (gc.nz + PZR - 1) / PZR);
         kRestrict2<T, false><<<grid, block, 0, c.stream>>>(gf, gc, rf, nullptr, nullptr, rc, c.S, c.rb, checkDone);
     }
@@ -1782,6 +1760,7 @@ int launchRestrict(const LaunchCtx& c, const Grid& gf, const Grid& gc, int div, 
 
 int launchUpdateRestrict(const LaunchCtx& c, const Grid& gf, const Grid& gc, const float* rIn, const float* Ap,
                          float* rOut, float* rc) {
+    if ((c.tma & 1) && launchRestrictTma(c, gf, gc, rIn, Ap, rOut, rc, 1)) return 1;
     dim3 block(32, 8), grid((gc.nx + 31) / 32, (gc.ny + 7) / 8, (gc.nz + PZR - 1) / PZR);
     kRestrict2<float, true><<<grid, block, 0, c.stream>>>(gf, gc, rIn, Ap, rOut, rc, c.S, c.rb, 1);
     return 1;
@@ -1807,6 +1786,9 @@ int launchProlongSmooth(const LaunchCtx& c, const Grid& gf, const Grid& gc, int 
         };
         if constexpr (std::is_same<T, float>::value) {
             if (half) {
+                if ((c.tma & 2) && launchProlongBulk(c, gf, gc, zc, rf, hd.d, flags, zf, coef * (double)hd.scale, maskFixed,
+                                               aux, epi, checkDone))
+                    return 1;
                 go(kProlongFlat<float, __half>, hd.d, coef * (double)hd.scale);
                 return 1;
             }

@@ -96,6 +96,7 @@ struct LaunchCtx {
     cudaStream_t stream;
     Scalars* S;
     RedBuf rb;
+    int tma = 0;  // bit 0: FP32 2x restrictions with TMA-staged rows; bit 1: bulk-staged mixed prolongation
 };
 
 // Opt the matvec kernels into > 48 KB of dynamic shared memory (once per device).
@@ -241,6 +242,21 @@ bool tcEligible(const MatvecArgs<float>& a);
 cudaError_t tcSetAttributes();
 int launchMatvecTC(const LaunchCtx& c, const MatvecArgs<float>& a, const TcOperand& op);
 int64_t tcBlocks(const Grid& g);  // reduction blocks of a launch
+
+// FP32 2x restriction with TMA-staged fine rows (transfer_tma.cu); Ap != null:
+// with the fused residual update (rOut = rIn - alpha Ap, r.r).  Returns 0 (and
+// launches nothing) when a tensor map cannot be made for the vectors.
+cudaError_t tmaSetAttributes();
+bool tmaAvailable(const float* v, int64_t n);  // a tensor map can be made for these n floats
+// The mixed V-cycle's 2x up-leg (kProlongFlat<float, __half> semantics) with its
+// ranges staged by bulk copies; the vectors must come from allocations with at
+// least 16 spare bytes past their end.  Returns 0 (nothing launched) for grids
+// whose ranges exceed the shared-memory budget.
+int launchProlongBulk(const LaunchCtx& c, const Grid& gf, const Grid& gc, const float* zc, const float* rf,
+                      const __half* dinv, const uint8_t* flags, float* zf, double coef, int maskFixed,
+                      const float* aux, int epi, int checkDone);
+int launchRestrictTma(const LaunchCtx& c, const Grid& gf, const Grid& gc, const float* rIn, const float* Ap,
+                      float* rOut, float* rc, int checkDone);
 
 // Device-side ``done`` / iteration snapshot is read back by the host with a plain copy.
 

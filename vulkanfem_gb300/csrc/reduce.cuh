@@ -138,5 +138,30 @@ __device__ __forceinline__ bool trueResidualDue(const Scalars* S) {
            (S->delta2 > 0.0 && S->rr < S->delta2 * S->rrLast);
 }
 
+// Per-thread dot-product accumulator.  FP64 vectors accumulate in FP64.  FP32
+// vectors accumulate in FP32 with Kahan compensation and are converted to FP64
+// once per thread, before the FP64 block and grid reduction: on GB300 the FP64
+// pipe is ~1/64 of FP32, so per-element FP64 conversions and FMAs would bound
+// the FP32 kernels.
+template <typename T>
+struct DotAcc;
+template <>
+struct DotAcc<double> {
+    double s = 0.0;
+    __device__ __forceinline__ void add(double v) { s += v; }
+    __device__ __forceinline__ double get() const { return s; }
+};
+template <>
+struct DotAcc<float> {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float v) {
+        const float y = v - c;
+        const float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ double get() const { return (double)s - (double)c; }
+};
+
 }  // namespace
 }  // namespace vfem
