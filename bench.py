@@ -179,11 +179,15 @@ def algorithmic_bytes(kind, g0, g1, s):
     modulus, fixed bits); restrict 3sN_f + 3sN_c; prolong+smooth 3sN_c + 9sN_f (z_c,
     r, D^-1 in; z out) + N_f/8; x/r update 18sN (x, r, p, Ap in; x, r out); p
     update 9sN.  The mixed solve defers x += alpha p (its FP32 x correction) to
-    the p update: r update 9sN, p update 15sN (z, p, x in; p, x out)."""
+    the p update: r update 9sN, p update 15sN (z, p, x in; p, x out).  With the
+    p update fused into the product (matvec_px): p_old, z, x in and p, x, Kp out
+    plus the modulus and bits, 18sN + Ne/8 + 4Ne + N/8."""
     N, Ne = g0["nodes"], g0["voxels"]
     Nc = g1["nodes"]
     if kind == "matvec":
         return 6 * s * N + Ne / 8 + 4 * Ne + N / 8
+    if kind == "matvec_px":
+        return 18 * s * N + Ne / 8 + 4 * Ne + N / 8
     if kind == "restrict":
         return 3 * s * N + 3 * s * Nc
     if kind == "prolong":
@@ -358,6 +362,9 @@ def main():
         "restrict": (ms["restrict_fp32" if mixed else "restrict_fp64"], 1),
         "update_p": (ms["update_p_fp32" if mixed else "update_p_fp64"], 1),
     }
+    if mixed and ms.get("matvec_fp32_px", 0) > 0:  # the solve runs the fused product instead
+        per_iter["matvec_px"] = (ms["matvec_fp32_px"], 1)
+        del per_iter["matvec"], per_iter["update_p"]
     dom_k = max(per_iter, key=lambda k: per_iter[k][0])
     kms = per_iter[dom_k][0]
     abytes = algorithmic_bytes(dom_k, g0, g1, s)

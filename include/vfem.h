@@ -161,6 +161,24 @@ vfem_status vfem_solve_device(vfem_problem* p, const vfem_options* opt, double* 
  * fixed rows zeroed. */
 vfem_status vfem_apply_operator(vfem_problem* p, const double* x, double* y);
 
+/* Deflation coarse space (no counterpart in the reference; deflated PCG after
+ * Saad, Yeung, Erhel and Guyomarc'h, SIAM J. Sci. Comput. 21 (2000), in the
+ * A-DEF2 form of Tang, Nabben, Vuik and Erlangga, J. Sci. Comput. 39 (2009)).
+ * V holds k <= 4 columns (compressed numbering, column j at V + j * 3 *
+ * num_nodes); entries at fixed DOFs are taken as 0.  Every later solve starts
+ * from x0 + V G^-1 V^T r0 (G = V^T K V, K V computed once here with the FP64
+ * product) and every later preconditioner application, in solves and in
+ * vfem_apply_preconditioner(_mixed), returns
+ *   z = M^-1 r + V G^-1 (V^T r - (KV)^T M^-1 r),
+ * with M^-1 the multigrid cycle (the identity for VFEM_MG_NONE).  For the
+ * residuals of such a solve (orthogonal to V) this keeps every search direction
+ * K-orthogonal to V, which cannot raise CG's effective condition number.  The
+ * learned coarse correction passes the network's predicted displacement here
+ * (vulkanfem_gb300/learned.py).  k = 0 removes it.  Storage: 2 k FP64 and 2 k
+ * FP32 dense level-0 vectors.  VFEM_ERR_INVALID_ARGUMENT if V has a non-finite
+ * entry or V^T K V is singular. */
+vfem_status vfem_problem_set_coarse_space(vfem_problem* p, const double* V, int32_t k);
+
 /* The same product as the mixed-precision solver applies it (no counterpart in
  * the reference): x rounded to FP32, y = K x with the fixed rows zeroed computed
  * in FP32 (on the tensor cores when vfem_problem_uses_tensor_cores is 1, else on
@@ -246,7 +264,9 @@ typedef enum vfem_kernel_class {
     VFEM_K_TRUE_RESIDUAL_DF = 12, /* f - K x on FP64 vectors in double-float arithmetic */
     VFEM_K_UPDATE_RESTRICT_MIXED = 13, /* mixed: r -= alpha Ap, r.r and the first restriction in one pass */
     VFEM_K_MATVEC_FP32_SIMT = 14, /* the FP32 CG product on the CUDA cores, whichever product the problem uses */
-    VFEM_K_COUNT = 15
+    VFEM_K_MATVEC_FP32_PX = 15,   /* the mixed solve's FP32 CG product with the direction update (p = z + beta p,
+                                     x += alpha p) fused into it; 0 ms when the problem does not use it */
+    VFEM_K_COUNT = 16
 } vfem_kernel_class;
 
 /* Measurement helper (no counterpart in the reference): average device time in

@@ -169,3 +169,36 @@ def test_forced_64bit_coarse_factorisation(small):
     assert rel(zb, za) < 1e-3
     u, st = B.solve(small["f"], precision="mixed")
     assert st["rel_residual"] < 1e-6 and rel(u, small["x_o"]) < 1e-5
+
+
+def test_fused_direction_update_is_bit_identical():
+    """The mixed solve's direction update fused into the CG product
+    (p = z + beta p_old and the deferred x += alpha p_old in the product's input
+    stage, alternating p buffers) against the separate update pass
+    (VFEM_FUSED_DIRECTION=0): the same arithmetic on the same values, so the
+    same iteration counts and bit-identical displacements, for the reference
+    and multiplicative cycles, plain and flexible CG, periodic residual
+    replacement, and the FP64 fallback after a forced breakdown.  The 40^3
+    field spans several product blocks in x, y and z."""
+    ke = domains.hex8_stiffness()
+    d = domains.training_field(40, seed=7, levels=3)
+    os.environ["VFEM_FUSED_DIRECTION"] = "0"
+    try:
+        B = api.assembleSystemMatrix(d.voxels, ke, d.fixed, 3)
+    finally:
+        os.environ.pop("VFEM_FUSED_DIRECTION", None)
+    A = api.assembleSystemMatrix(d.voxels, ke, d.fixed, 3)
+    ms = api.profile_kernels(A, 1)
+    assert ms["matvec_fp32_px"] > 0 and api.profile_kernels(B, 1)["matvec_fp32_px"] == 0
+    f = d.load_vector()
+    cases = [dict(), dict(mg_mode="vcycle"), dict(mg_mode="none"), dict(flexible=True),
+             dict(replace_every=7), dict(debug_break_at=9)]
+    for opts in cases:
+        ua, sa = A.solve(f, precision="mixed", **opts)
+        ub, sb = B.solve(f, precision="mixed", **opts)
+        assert sa["iterations"] == sb["iterations"], (opts, sa["iterations"], sb["iterations"])
+        assert sa["fallback"] == sb["fallback"]
+        assert np.array_equal(ua, ub), (opts, rel(ua, ub))
+        assert sa["rel_residual"] < 1e-6
+    A.close()
+    B.close()

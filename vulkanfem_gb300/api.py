@@ -44,7 +44,7 @@ EXPORTED = (
     "vfem_restrict", "vfem_interpolate", "vfem_inverse_diagonal", "vfem_fixed_nodes",
     "vfem_kernel_launch_count", "vfem_last_error_message", "vfem_profile_kernels",
     "vfem_apply_operator_device_noalloc", "vfem_apply_operator_mixed", "vfem_problem_uses_tensor_cores",
-    "vfem_problem_uses_tma",
+    "vfem_problem_uses_tma", "vfem_problem_set_coarse_space",
     # learned warm start (include/vfem_net.h)
     "vfem_net_create", "vfem_net_destroy", "vfem_net_num_params", "vfem_net_set_params", "vfem_net_get_params",
     "vfem_net_forward", "vfem_net_train_batch", "vfem_net_last_error_message",
@@ -52,7 +52,8 @@ EXPORTED = (
 
 KERNEL_CLASSES = ("matvec_fp64", "matvec_fp32", "restrict_fp64", "restrict_fp32", "prolong_fp64", "prolong_fp32",
                   "update_xr_fp64", "update_xr_mixed", "update_p_fp64", "update_p_fp32", "coarse_fp64",
-                  "coarse_fp32", "true_residual_df", "update_restrict_mixed", "matvec_fp32_simt")
+                  "coarse_fp32", "true_residual_df", "update_restrict_mixed", "matvec_fp32_simt",
+                  "matvec_fp32_px")
 
 
 class VfemError(RuntimeError):
@@ -136,6 +137,7 @@ def load_library(build_if_missing=True):
     lib.vfem_apply_operator_mixed.argtypes = [P, f64p, f64p, ctypes.c_void_p]
     lib.vfem_problem_uses_tensor_cores.argtypes = [P]
     lib.vfem_problem_uses_tensor_cores.restype = ctypes.c_int32
+    lib.vfem_problem_set_coarse_space.argtypes = [P, ctypes.c_void_p, i32]
     lib.vfem_problem_uses_tma.argtypes = [P]
     lib.vfem_problem_uses_tma.restype = ctypes.c_int32
     for name in EXPORTED:
@@ -266,6 +268,23 @@ class MatrixFreeSparse:
         return y
 
     __matmul__ = dot
+
+    def set_coarse_space(self, V=None):
+        """Deflation coarse space for every later solve and preconditioner
+        application (V: [rows] or [rows, k], k <= 4; entries at fixed DOFs are
+        taken as 0; None removes it).  The preconditioner becomes
+        M^-1 r + V G^-1 (V^T r - (KV)^T M^-1 r), G = V^T K V, and PCG starts
+        from x0 + V G^-1 V^T r0."""
+        if V is None:
+            _check(self._lib.vfem_problem_set_coarse_space(self._h, None, 0))
+            return
+        V = np.asarray(V, np.float64)
+        if V.ndim == 1:
+            V = V[:, None]
+        if V.shape[0] != self.rows() or not 1 <= V.shape[1] <= 4:
+            raise VfemError(1, "coarse space must be [rows, k] with k <= 4")
+        cols = np.ascontiguousarray(V.T)
+        _check(self._lib.vfem_problem_set_coarse_space(self._h, cols.ctypes.data_as(ctypes.c_void_p), V.shape[1]))
 
     def dot_mixed(self, x):
         """The mixed-precision solver's product: FP32 (tensor cores when

@@ -18,6 +18,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <cstddef>
 #include <cstring>
 #include <map>
 #include <string>
@@ -111,6 +112,7 @@ struct vfem_problem {
     float *p32 = nullptr, *Ap32 = nullptr;
     float* x32 = nullptr;  // mixed precision: FP32 solution correction since the last FP64 flush
     float* r32b = nullptr;  // mixed precision: the level-0 residual alternates between L[0].r32 and this
+    float* p32b = nullptr;  // fused direction update: the FP32 direction alternates between p32 and this
     // coarsest dense inverse
     int64_t nc = 0;
     int32_t* freeDof = nullptr;
@@ -145,6 +147,14 @@ struct vfem_problem {
     TcOperand tc;
     bool tcReady = false;
     int tma = 0;  // bit 0: TMA-staged FP32 restrictions, bit 1: bulk-staged mixed prolongation (LaunchCtx::tma)
+    bool pxFused = false;  // mixed solve: direction update fused into the CG product (launchMatvecPX)
+    // deflation coarse space (vfem_problem_set_coarse_space): k dense columns V and K V
+    int coarseK = 0, coarseCap = 0;
+    double* V64 = nullptr;
+    float* V32 = nullptr;
+    double* KV64 = nullptr;
+    float* KV32 = nullptr;
+    CoarseSpace coarseG{};
     std::map<GraphKey, CachedGraph> graphs;
     bool rhsSet = false;
     long long launches = 0;
@@ -205,10 +215,10 @@ void freeProblem(vfem_problem* p) {
         cudaFree(l.r64); cudaFree(l.z64); cudaFree(l.t64); cudaFree(l.r32); cudaFree(l.z32); cudaFree(l.t32);
     }
     cudaFree(p->f64); cudaFree(p->x64); cudaFree(p->p64); cudaFree(p->Ap64); cudaFree(p->p32); cudaFree(p->Ap32);
-    cudaFree(p->x32); cudaFree(p->r32b);
+    cudaFree(p->x32); cudaFree(p->r32b); cudaFree(p->p32b);
     cudaFree(p->freeDof); cudaFree(p->Kinv64); cudaFree(p->KinvH); cudaFree(p->cb64); cudaFree(p->cb32);
     cudaFree(p->KinvV64); cudaFree(p->KinvVH); cudaFree(p->dFreeNode); cudaFree(p->cpart);
-    cudaFree(p->dFlag);
+    cudaFree(p->dFlag); cudaFree(p->V64); cudaFree(p->V32); cudaFree(p->KV64); cudaFree(p->KV32);
     cudaFree(p->S); cudaFree(p->rb.partials); cudaFree(p->rb.ticket); cudaFree(p->dComp);
     if (p->hS) cudaFreeHost(p->hS);
     if (p->hIn) cudaFreeHost(p->hIn);
@@ -710,6 +720,10 @@ vfem_status createImpl(const uint8_t* vox, int nx, int ny, int nz, const double*
     // VFEM_TMA_MASK (default 0): bit 0 the FP32 restrictions with TMA-staged rows, bit 1 the
     // mixed up-leg with bulk-staged ranges; both measured slower than the direct-load kernels
     p->tma = tmaSetAttributes() == cudaSuccess ? (int)envInt("VFEM_TMA_MASK", 0) & 3 : 0;
+    // The mixed solve's direction update (p = z + beta p, x += alpha p) runs inside
+    // the CUDA-core CG product's input stage; VFEM_FUSED_DIRECTION=0 keeps the
+    // separate kUpdatePX pass (the general-Ke and tensor-core products always do).
+    p->pxFused = envInt("VFEM_FUSED_DIRECTION", 1) != 0 && p->ke.structured && !p->tcReady;
     st = buildHierarchyDevice(p, plan, vox, E, fixed, nfixed);
     if (st != VFEM_OK) return bail(st);
     for (DevLevel& d : p->L) {
@@ -720,9 +734,10 @@ vfem_status createImpl(const uint8_t* vox, int nx, int ny, int nz, const double*
     int64_t nv0 = p->L[0].nvec();
     CKP(dalloc(&p->f64, nv0)); CKP(dalloc(&p->x64, nv0)); CKP(dalloc(&p->p64, nv0)); CKP(dalloc(&p->Ap64, nv0));
     CKP(dalloc(&p->p32, nv0)); CKP(dalloc(&p->Ap32, nv0)); CKP(dalloc(&p->x32, nv0)); CKP(dalloc(&p->r32b, nv0));
+    if (p->pxFused) CKP(dalloc(&p->p32b, nv0));
     if (!tmaAvailable(p->r32b, nv0)) p->tma &= ~1;
     CKP(dalloc(&p->S, 1));
-    CKP(dalloc(&p->rb.partials, 2 * (int64_t)kMaxRedBlocks));
+    CKP(dalloc(&p->rb.partials, (int64_t)kMaxRedTerms * kMaxRedBlocks));
     CKP(dalloc(&p->rb.ticket, 1));
     CKP(dalloc(&p->dComp, 3 * p->L[0].nused));
     CKP(dalloc(&p->dFlag, 1));
@@ -900,18 +915,37 @@ int vcycle(vfem_problem* p, const vfem_options& o, int lv, T* r, T* z, T** outZ,
     return n;
 }
 
-// Preconditioner application on level 0 (identity when mg_mode == NONE).
+template <typename T>
+const T* coarseV(vfem_problem* p, bool kv);
+template <>
+const double* coarseV<double>(vfem_problem* p, bool kv) { return kv ? p->KV64 : p->V64; }
+template <>
+const float* coarseV<float>(vfem_problem* p, bool kv) { return kv ? p->KV32 : p->V32; }
+
+// Preconditioner application on level 0 (identity when mg_mode == NONE).  With a
+// coarse space V set, the result is the deflated (A-DEF2) form
+//   z = M^-1 r + V G^-1 (V^T r - (KV)^T M^-1 r),  G = V^T K V,
+// which for residuals orthogonal to V (those of deflated CG) is the projection
+// (I - V G^-1 V^T K) M^-1 r that keeps every search direction K-orthogonal to V;
+// the dots of `epi` (r.z, z.aux) are then taken on that z.
 template <typename T>
 int precondition(vfem_problem* p, const vfem_options& o, T* r, T* z, T** outZ, const T* aux, int epi,
                  bool restricted = false) {
+    DevLevel& l = p->L[0];
+    const bool cs = p->coarseK > 0;
+    int n = 0;
     if (o.mg_mode == VFEM_MG_NONE) {
-        DevLevel& l = p->L[0];
-        int n = launchConvert<T, T>(p->stream, l.nvec(), r, z);
-        n += launchDots<T>(ctx(p), l.nvec(), r, z, aux ? z : nullptr, aux, epi, 1);
+        n = launchConvert<T, T>(p->stream, l.nvec(), r, z);
         *outZ = z;
-        return n;
+    } else {
+        n = vcycle<T>(p, o, 0, r, z, outZ, cs ? nullptr : aux, cs ? EPI_NONE : epi, restricted);
+        if (!cs) return n;
     }
-    return vcycle<T>(p, o, 0, r, z, outZ, aux, epi, restricted);
+    if (cs)
+        n += launchCoarseSpace<T>(ctx(p), l.nvec(), p->coarseK, coarseV<T>(p, false), coarseV<T>(p, true), p->coarseG,
+                                  r, *outZ, 1);
+    if (epi != EPI_NONE) n += launchDots<T>(ctx(p), l.nvec(), r, *outZ, aux ? *outZ : nullptr, aux, epi, 1);
+    return n;
 }
 
 // The mixed solve fuses its residual update with the first restriction of the
@@ -942,8 +976,16 @@ int iteration(vfem_problem* p, const vfem_options& o, double** zOut64, float** z
         MatvecArgs<float> a = mvArgs<float>(p, 0, p->p32, p->Ap32, MV_AX);
         a.dot0 = DOT_X_OUT;
         a.epi = EPI_ALPHA;
-        k += matvec<float>(p, a);
-        // x += alpha p is deferred to launchUpdatePX / the flush
+        if (p->pxFused) {
+            // p = z + beta p and the previous iteration's x += alpha p, in the product
+            a.zin = *zOut32;
+            a.pAlt = p->p32b;
+            a.xacc = p->x32;
+            k += launchMatvecPX(c, a, static_cast<const float*>(opc<float>(p)));
+        } else {
+            k += matvec<float>(p, a);
+        }
+        // x += alpha p is deferred to the next product (or launchUpdatePX) / the flush
         const bool fused = fusedUpdateRestrict(p, o);
         float* r = l0.r32;
         if (fused) {
@@ -953,7 +995,7 @@ int iteration(vfem_problem* p, const vfem_options& o, double** zOut64, float** z
         } else {
             k += launchUpdateR(c, n, r, p->Ap32);
         }
-        k += launchFlushX(c, n, p->x64, p->x32, p->p32, 1);
+        k += launchFlushX(c, n, p->x64, p->x32, p->p32, p->p32b, 1);
         // True residual f - K x64 in double-float; only its FP32 rounding (the new
         // recursive residual) and its norm are kept.
         MatvecArgs<double> t = mvArgs<double>(p, 0, p->x64, nullptr, MV_RESID);
@@ -967,7 +1009,7 @@ int iteration(vfem_problem* p, const vfem_options& o, double** zOut64, float** z
         if (fused) k += launchRestrict<float>(c, l0.g, p->L[1].g, 2, r, p->L[1].r32, 2);
         float* z = nullptr;
         k += precondition<float>(p, o, r, l0.z32, &z, o.flexible ? p->Ap32 : nullptr, EPI_BETA, fused);
-        k += launchUpdatePX(c, n, p->p32, z, p->x32);
+        if (!p->pxFused) k += launchUpdatePX(c, n, p->p32, z, p->x32);
         *zOut32 = z;
     }
     return k;
@@ -1018,11 +1060,17 @@ vfem_status solvePhase(vfem_problem* p, const vfem_options& o, bool haveX0, vfem
         launches += launchConvert<double, double>(p->stream, n, p->f64, l0.r64);
         if (mixed) launches += launchConvert<double, float>(p->stream, n, p->f64, l0.r32);
     }
+    if (p->coarseK > 0) {
+        // deflated CG starts from x + V G^-1 V^T r, whose residual is orthogonal to V
+        launches += launchCoarseStart(c, n, p->coarseK, p->V64, p->KV64, p->coarseG, p->x64, l0.r64);
+        if (mixed) launches += launchConvert<double, float>(p->stream, n, l0.r64, l0.r32);
+    }
     if (mixed) launches += launchFill<float>(p->stream, n, p->x32, 0.f);
     launches += launchDots<double>(c, n, p->f64, p->f64, l0.r64, l0.r64, EPI_INIT, 0);
     if (mixed) {
         launches += precondition<float>(p, o, l0.r32, l0.z32, &z32, nullptr, EPI_RHO0);
-        launches += launchUpdateP<float>(c, n, p->p32, z32, 1);
+        // (fused: the first product forms p = z, beta being 0 in fresh scalars)
+        if (!p->pxFused) launches += launchUpdateP<float>(c, n, p->p32, z32, 1);
     } else {
         launches += precondition<double>(p, o, l0.r64, l0.z64, &z64, nullptr, EPI_RHO0);
         launches += launchUpdateP<double>(c, n, p->p64, z64, 1);
@@ -1070,7 +1118,7 @@ vfem_status solvePhase(vfem_problem* p, const vfem_options& o, bool haveX0, vfem
         parity ^= flip;
         ++chunks;
     }
-    if (mixed) launches += launchFlushX(c, n, p->x64, p->x32, p->p32, 0);  // fold the remaining correction
+    if (mixed) launches += launchFlushX(c, n, p->x64, p->x32, p->p32, p->p32b, 0);  // fold the remaining correction
     CK(cudaEventRecord(e1, p->stream));
     CK(cudaEventSynchronize(e1));
     float ms = 0;
@@ -1376,6 +1424,93 @@ vfem_status vfem_apply_operator_mixed(vfem_problem* p, const double* x, double* 
     return VFEM_OK;
 }
 
+vfem_status vfem_problem_set_coarse_space(vfem_problem* p, const double* V, int32_t k) {
+    if (!p || k < 0 || k > 4 || (k > 0 && !V)) return fail(VFEM_ERR_INVALID_ARGUMENT, "bad argument");
+    CK(cudaSetDevice(p->device));
+    DevLevel& l0 = p->L[0];
+    const int64_t n = l0.nvec(), nc = 3 * l0.nused;
+    for (auto& kv : p->graphs)  // captured graphs hold the old correction
+        if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+    p->graphs.clear();
+    p->coarseK = 0;
+    if (k == 0) return VFEM_OK;
+    if (p->coarseCap < k) {
+        cudaFree(p->V64); cudaFree(p->V32); cudaFree(p->KV64); cudaFree(p->KV32);
+        p->V64 = p->KV64 = nullptr;
+        p->V32 = p->KV32 = nullptr;
+        p->coarseCap = 0;
+        CK(dalloc(&p->V64, k * n));
+        CK(dalloc(&p->V32, k * n));
+        CK(dalloc(&p->KV64, k * n));
+        CK(dalloc(&p->KV32, k * n));
+        p->coarseCap = k;
+    }
+    // columns with their fixed DOFs zeroed (the space the solver's iterates live in)
+    int64_t nfix = 0;
+    vfem_status s = vfem_fixed_nodes(p, 0, nullptr, 0, &nfix);
+    if (s != VFEM_OK) return s;
+    std::vector<int64_t> fixedNodes((size_t)nfix);
+    if (nfix > 0 && (s = vfem_fixed_nodes(p, 0, fixedNodes.data(), nfix, &nfix)) != VFEM_OK) return s;
+    std::vector<double> Vm(V, V + (size_t)nc * k);
+    for (int j = 0; j < k; ++j)
+        for (int64_t id : fixedNodes)
+            for (int c3 = 0; c3 < 3; ++c3) Vm[(size_t)j * nc + 3 * id + c3] = 0.0;
+    // K V from the FP64 operator (fixed rows zeroed), then G = V^T K V on the host
+    std::vector<double> KV((size_t)nc * k);
+    for (int j = 0; j < k; ++j) {
+        double* vj = p->V64 + (size_t)j * n;
+        double* kvj = p->KV64 + (size_t)j * n;
+        s = toDenseHost(p, 0, Vm.data() + (size_t)j * nc, vj, true);
+        if (s != VFEM_OK) return s;
+        MatvecArgs<double> a = mvArgs<double>(p, 0, vj, kvj, MV_AX);
+        a.checkDone = 0;
+        p->launches += matvec<double>(p, a);
+        s = fromDenseHost(p, 0, kvj, KV.data() + (size_t)j * nc);
+        if (s != VFEM_OK) return s;
+        unsigned bad = 0;
+        CK(cudaMemcpyAsync(&bad, p->dFlag, sizeof(unsigned), cudaMemcpyDeviceToHost, p->stream));
+        CK(cudaStreamSynchronize(p->stream));
+        if (bad) return fail(VFEM_ERR_INVALID_ARGUMENT, "coarse space: non-finite entry");
+    }
+    p->launches += launchConvert<double, float>(p->stream, k * n, p->V64, p->V32);
+    p->launches += launchConvert<double, float>(p->stream, k * n, p->KV64, p->KV32);
+    CK(cudaStreamSynchronize(p->stream));
+    double G[16] = {0}, Gi[16] = {0};
+    for (int a = 0; a < k; ++a)
+        for (int b = 0; b < k; ++b) {
+            double sum = 0.0;
+            for (int64_t i = 0; i < nc; ++i) sum += Vm[(size_t)a * nc + i] * KV[(size_t)b * nc + i];
+            G[4 * a + b] = sum;
+        }
+    // symmetrise, then invert by Gauss-Jordan with partial pivoting (k <= 4)
+    double M[4][8] = {};
+    for (int a = 0; a < k; ++a)
+        for (int b = 0; b < k; ++b) {
+            M[a][b] = 0.5 * (G[4 * a + b] + G[4 * b + a]);
+            M[a][4 + b] = a == b ? 1.0 : 0.0;
+        }
+    for (int c = 0; c < k; ++c) {
+        int piv = c;
+        for (int r2 = c + 1; r2 < k; ++r2)
+            if (std::fabs(M[r2][c]) > std::fabs(M[piv][c])) piv = r2;
+        if (!(M[piv][c] > 0.0 || M[piv][c] < 0.0) || !std::isfinite(M[piv][c]))
+            return fail(VFEM_ERR_INVALID_ARGUMENT, "coarse space: V^T K V is singular (dependent or fixed-only columns)");
+        for (int q = 0; q < 8; ++q) std::swap(M[c][q], M[piv][q]);
+        const double d = M[c][c];
+        for (int q = 0; q < 8; ++q) M[c][q] /= d;
+        for (int r2 = 0; r2 < k; ++r2)
+            if (r2 != c) {
+                const double f = M[r2][c];
+                for (int q = 0; q < 8; ++q) M[r2][q] -= f * M[c][q];
+            }
+    }
+    for (int a = 0; a < k; ++a)
+        for (int b = 0; b < k; ++b) Gi[4 * a + b] = M[a][4 + b];
+    std::memcpy(p->coarseG.Ginv, Gi, sizeof(Gi));
+    p->coarseK = k;
+    return VFEM_OK;
+}
+
 int32_t vfem_problem_uses_tensor_cores(const vfem_problem* p) { return p && p->tcReady ? 1 : 0; }
 
 int32_t vfem_problem_uses_tma(const vfem_problem* p) { return p ? p->tma : 0; }
@@ -1410,7 +1545,7 @@ vfem_status vfem_apply_preconditioner(vfem_problem* p, int32_t mg_mode, const do
     o.mg_mode = mg_mode;
     launchInitScalars(p->stream, p->S, 1e-6, 1, 0, 0, 0, 0.0);
     double* zo = nullptr;
-    int k = 1 + vcycle<double>(p, o, 0, l0.r64, l0.z64, &zo, nullptr, EPI_NONE);
+    int k = 1 + precondition<double>(p, o, l0.r64, l0.z64, &zo, nullptr, EPI_NONE);
     p->launches += k;
     g_launches += k;
     CK(cudaGetLastError());
@@ -1434,7 +1569,7 @@ vfem_status vfem_apply_preconditioner_mixed(vfem_problem* p, int32_t mg_mode, co
     int k = launchConvert<double, float>(p->stream, n, l0.r64, l0.r32);
     k += launchInitScalars(p->stream, p->S, 1e-6, 1, 0, 1, 0, 0.0);
     float* zo = nullptr;
-    k += vcycle<float>(p, o, 0, l0.r32, l0.z32, &zo, nullptr, EPI_NONE);
+    k += precondition<float>(p, o, l0.r32, l0.z32, &zo, nullptr, EPI_NONE);
     k += launchConvert<float, double>(p->stream, n, zo, l0.z64);
     p->launches += k;
     g_launches += k;
@@ -1495,9 +1630,30 @@ vfem_status vfem_profile_kernels(vfem_problem* p, int32_t reps, double* ms) {
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
     long long launched = 1;
+    bool pxScalars = false;
     for (int k = 0; k < VFEM_K_COUNT; ++k) {
         auto one = [&]() -> int {
             switch (k) {
+                case VFEM_K_MATVEC_FP32_PX: {
+                    if (!p->pxFused) return 0;
+                    if (!pxScalars) {  // nonzero alpha and beta: the update runs in full (first, untimed call)
+                        static const double half = 0.5;
+                        char* sb = reinterpret_cast<char*>(p->S);
+                        if (cudaMemcpyAsync(sb + offsetof(Scalars, alpha), &half, sizeof(double),
+                                            cudaMemcpyHostToDevice, p->stream) != cudaSuccess ||
+                            cudaMemcpyAsync(sb + offsetof(Scalars, beta), &half, sizeof(double),
+                                            cudaMemcpyHostToDevice, p->stream) != cudaSuccess)
+                            return 0;
+                        pxScalars = true;
+                    }
+                    MatvecArgs<float> a = mvArgs<float>(p, 0, p->p32, p->Ap32, MV_AX);
+                    a.dot0 = DOT_X_OUT;
+                    a.epi = EPI_STORE;
+                    a.zin = l0.z32;
+                    a.pAlt = p->p32b;
+                    a.xacc = p->x32;
+                    return launchMatvecPX(c, a, static_cast<const float*>(opc<float>(p)));
+                }
                 case VFEM_K_MATVEC_FP64: {
                     MatvecArgs<double> a = mvArgs<double>(p, 0, p->p64, p->Ap64, MV_AX);
                     a.dot0 = DOT_X_OUT;

@@ -520,8 +520,16 @@ __device__ __forceinline__ void foldCarry<float>(const float (&y)[24], float (&c
 //   OUT_CG    the CG product: y = Kx (fixed rows 0), dot x.(Kx); the per-thread
 //             dot sums at most 48 terms and accumulates with plain FMAs;
 //   OUT_TRUE  the true residual: r = f - Kx, its FP32 rounding to y32, y (FP64)
-//             only when given, dot r.r.
-enum MvOut : int { OUT_ANY = 0, OUT_CG = 1, OUT_TRUE = 2 };
+//             only when given, dot r.r;
+//   OUT_CG_PX the CG product with the mixed solve's direction update fused into
+//             the input stage: every staged node value is p = z + beta p_old
+//             (halo copies computed the same way by every block that stages
+//             them), and the thread that stages an owned node writes the new p
+//             to the other p buffer and adds the deferred alpha p_old to the
+//             FP32 solution correction.  The p buffers alternate (Scalars::pSel,
+//             flipped by the last block), because neighbouring blocks still read
+//             p_old as their halo.
+enum MvOut : int { OUT_ANY = 0, OUT_CG = 1, OUT_TRUE = 2, OUT_CG_PX = 3 };
 template <typename T, typename TC, int OUT = OUT_ANY>
 __global__ void __launch_bounds__(MV_TX* MV_TY, sizeof(TC) == 4 ? 3 : 2)
     kMatvecH(MatvecArgs<T> a, const Ks<TC> kp, Scalars* S, RedBuf rb) {
@@ -551,27 +559,84 @@ __global__ void __launch_bounds__(MV_TX* MV_TY, sizeof(TC) == 4 ? 3 : 2)
     const bool okC = hasC && cX >= 0 && cX < g.nx && cY >= 0 && cY < g.ny;
 #define SU(b, iy, ix) (su + (((((b) * (MV_TY + 1)) + (iy)) * (MV_TX + 1) + (ix)) << 2))
 #define SY(k, iy, ix) (sy + (((((k) * MV_TY) + (iy)) * MV_TX + (ix)) << 2))
+    // Input source; OUT_CG_PX: p_old, the buffer for the new p, beta and the
+    // deferred alpha (0 when a flush has folded it).  Every block reads the
+    // scalars here, before it reaches the grid reduction after which the last
+    // block flips pSel and advances matvecs.
+    const T* src = a.x;
+    T* pNew = nullptr;
+    T beta = T(0), ax = T(0);
+    int sel = 0;
+    if constexpr (OUT == OUT_CG_PX) {
+        sel = S->pSel;
+        src = sel ? a.pAlt : a.x;
+        pNew = sel ? const_cast<T*>(a.x) : a.pAlt;
+        beta = T(S->beta);
+        ax = S->foldStamp == S->matvecs ? T(0) : T(S->alpha);
+        if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && tx == 0 && ty == 0)
+            S->pxStamp = S->matvecs;  // read only by kFlushX
+    }
+    // The thread that stages node (ecx, ecy) is the one after its owner in x and y.
+    // OUT_CG_PX keeps the raw z, p_old (and, for an owned node, x) values of the
+    // prefetched layer in registers and forms p = z + beta p_old when the layer
+    // is staged to shared memory, so the prefetch stays in flight across the
+    // element computation as in the plain product.
+    const bool stagesOwned = OUT == OUT_CG_PX && tx >= 1 && ty >= 1;
     T pf[9];
+    [[maybe_unused]] T pq[OUT == OUT_CG_PX ? 9 : 1], xq[OUT == OUT_CG_PX ? 3 : 1];
+    auto ld3 = [&](int64_t i, int o) {
+        pf[o] = src[i];
+        pf[o + 1] = src[i + 1];
+        pf[o + 2] = src[i + 2];
+        if constexpr (OUT == OUT_CG_PX) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                pq[o + c] = pf[o + c];
+                pf[o + c] = a.zin[i + c];
+            }
+        }
+    };
+    auto ownsLayer = [&](int zl) { return stagesOwned && ok0 && zl >= z0 && zl < zend; };
     auto gload = [&](int zl) {
         const bool zok = zl >= 0 && zl < g.nz;
         const int64_t zoff = (int64_t)zl * plane;
 #pragma unroll
         for (int i = 0; i < 9; ++i) pf[i] = T(0);
+        if constexpr (OUT == OUT_CG_PX) {
+#pragma unroll
+            for (int i = 0; i < 9; ++i) pq[i] = T(0);
+        }
         if (ok0 && zok) {
-            const T* p = a.x + 3 * ((int64_t)eCol + zoff);
-            pf[0] = p[0]; pf[1] = p[1]; pf[2] = p[2];
+            ld3(3 * ((int64_t)eCol + zoff), 0);
+            if constexpr (OUT == OUT_CG_PX) {
+                if (ax != T(0) && ownsLayer(zl)) {
+                    const int64_t i = 3 * ((int64_t)eCol + zoff);
+                    xq[0] = a.xacc[i];
+                    xq[1] = a.xacc[i + 1];
+                    xq[2] = a.xacc[i + 2];
+                }
+            }
         }
-        if (okR && zok) {
-            const T* p = a.x + 3 * ((int64_t)(rY * g.nx + rX) + zoff);
-            pf[3] = p[0]; pf[4] = p[1]; pf[5] = p[2];
-        }
-        if (okC && zok) {
-            const T* p = a.x + 3 * ((int64_t)(cY * g.nx + cX) + zoff);
-            pf[6] = p[0]; pf[7] = p[1]; pf[8] = p[2];
-        }
+        if (okR && zok) ld3(3 * ((int64_t)(rY * g.nx + rX) + zoff), 3);
+        if (okC && zok) ld3(3 * ((int64_t)(cY * g.nx + cX) + zoff), 6);
     };
     auto sstore = [&](int zl) {
         const int b = zl & 1;
+        if constexpr (OUT == OUT_CG_PX) {
+            if (beta != T(0)) {
+#pragma unroll
+                for (int i = 0; i < 9; ++i) pf[i] = fma(beta, pq[i], pf[i]);
+            }
+            if (ownsLayer(zl)) {
+                const int64_t i = 3 * ((int64_t)eCol + (int64_t)zl * plane);
+#pragma unroll
+                for (int c = 0; c < 3; ++c) pNew[i + c] = pf[c];
+                if (ax != T(0)) {
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) a.xacc[i + c] = fma(ax, pq[c], xq[c]);
+                }
+            }
+        }
         stSlot<TC>(SU(b, ty, tx), C::in(pf[0]), C::in(pf[1]), C::in(pf[2]));
         if (hasR) stSlot<TC>(SU(b, MV_TY, tx), C::in(pf[3]), C::in(pf[4]), C::in(pf[5]));
         if (hasC) stSlot<TC>(SU(b, tx, MV_TX), C::in(pf[6]), C::in(pf[7]), C::in(pf[8]));
@@ -649,7 +714,7 @@ __global__ void __launch_bounds__(MV_TX* MV_TY, sizeof(TC) == 4 ? 3 : 2)
 #pragma unroll
             for (int c = 0; c < 3; ++c) sum[c] += q[c];
             const int64_t s = (int64_t)oCol + (int64_t)k * plane;
-            if constexpr (OUT == OUT_CG) {
+            if constexpr (OUT == OUT_CG || OUT == OUT_CG_PX) {
                 const bool fixed = (fl & FLAG_FIXED) != 0;
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
@@ -673,10 +738,13 @@ __global__ void __launch_bounds__(MV_TX* MV_TY, sizeof(TC) == 4 ? 3 : 2)
     }
 #undef SU
 #undef SY
-    if constexpr (OUT == OUT_CG) d0.add(dAx);
+    if constexpr (OUT == OUT_CG || OUT == OUT_CG_PX) d0.add(dAx);
     if (a.epi != EPI_NONE) {
         double v[2] = {d0.get(), d1.get()}, t[2];
-        if (gridReduce<MV_TX * MV_TY, 2>(v, rb, t)) applyEpi(a.epi, S, t[0], t[1]);
+        if (gridReduce<MV_TX * MV_TY, 2>(v, rb, t)) {
+            applyEpi(a.epi, S, t[0], t[1]);
+            if constexpr (OUT == OUT_CG_PX) S->pSel = sel ^ 1;
+        }
     }
 }
 
@@ -1520,8 +1588,10 @@ __global__ void __launch_bounds__(256) kUpdateR(int64_t n, float* __restrict__ r
 // last iteration): alpha p only if kUpdateR ran in the last iteration and
 // neither a flush nor kUpdatePX has folded it.
 __global__ void __launch_bounds__(256) kFlushX(int64_t n, double* __restrict__ x64, float* __restrict__ x32,
-                                               const float* __restrict__ p, Scalars* S, int conditional) {
+                                               const float* __restrict__ pFirst, const float* __restrict__ pSecond,
+                                               Scalars* S, int conditional) {
     if (conditional && (S->done || !trueResidualDue(S))) return;
+    const float* __restrict__ p = S->pSel ? pSecond : pFirst;
     const bool pending =
         conditional || (S->rStamp == S->matvecs && S->foldStamp != S->matvecs && S->pxStamp != S->matvecs);
     const double a = pending ? S->alpha : 0.0;
@@ -1591,6 +1661,72 @@ __global__ void __launch_bounds__(256) kDots(int64_t n, const T* __restrict__ a,
     }
     double v[2] = {s0.get(), s1.get()}, t[2];
     if (gridReduce<NT, 2>(v, rb, t)) applyEpi(epi, S, t[0], t[1]);
+}
+
+// Deflation coarse space, part 1: t_j = v_j . r - (K v_j) . z (j < k; z may be
+// null), reduced over the grid; the last block stores G^-1 t in the solver scalars.
+template <typename T>
+__global__ void __launch_bounds__(256) kCoarseDots(int64_t n, int k, const T* __restrict__ V,
+                                                   const T* __restrict__ KV, const T* __restrict__ r,
+                                                   const T* __restrict__ z, CoarseSpace G, Scalars* S, RedBuf rb,
+                                                   int checkDone) {
+    if (checkDone && S->done) return;
+    DotAcc<T> acc[4];
+    for (int64_t i = blockIdx.x * (int64_t)NT + threadIdx.x; i < n; i += (int64_t)gridDim.x * NT) {
+        const T ri = r[i];
+        const T zi = z ? z[i] : T(0);
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (j < k) {
+                acc[j].add(V[(int64_t)j * n + i] * ri);
+                if (z) acc[j].add(-KV[(int64_t)j * n + i] * zi);
+            }
+    }
+    double v[4] = {acc[0].get(), acc[1].get(), acc[2].get(), acc[3].get()}, t[4];
+    if (gridReduce<NT, 4>(v, rb, t)) {
+        for (int a = 0; a < 4; ++a) {
+            double sum = 0.0;
+            for (int b = 0; b < k; ++b) sum += G.Ginv[4 * a + b] * t[b];
+            S->coarseCoef[a] = a < k ? sum : 0.0;
+        }
+    }
+}
+
+// Part 2: z += sum_j coef_j v_j.
+template <typename T>
+__global__ void __launch_bounds__(256) kCoarseAxpy(int64_t n, int k, const T* __restrict__ V, T* __restrict__ z,
+                                                   const Scalars* S, int checkDone) {
+    if (checkDone && S->done) return;
+    T cf[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) cf[j] = (T)S->coarseCoef[j];
+    for (int64_t i = blockIdx.x * (int64_t)NT + threadIdx.x; i < n; i += (int64_t)gridDim.x * NT) {
+        T zi = z[i];
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (j < k) zi = fma(cf[j], V[(int64_t)j * n + i], zi);
+        z[i] = zi;
+    }
+}
+
+// Start projection: x += sum_j mu_j v_j, r -= sum_j mu_j (K v_j).
+__global__ void __launch_bounds__(256) kCoarseStart(int64_t n, int k, const double* __restrict__ V,
+                                                    const double* __restrict__ KV, const Scalars* S,
+                                                    double* __restrict__ x, double* __restrict__ r) {
+    double mu[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) mu[j] = S->coarseCoef[j];
+    for (int64_t i = blockIdx.x * (int64_t)NT + threadIdx.x; i < n; i += (int64_t)gridDim.x * NT) {
+        double xi = x[i], ri = r[i];
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (j < k) {
+                xi = fma(mu[j], V[(int64_t)j * n + i], xi);
+                ri = fma(-mu[j], KV[(int64_t)j * n + i], ri);
+            }
+        x[i] = xi;
+        r[i] = ri;
+    }
 }
 
 template <typename TI, typename TO>
@@ -1692,6 +1828,7 @@ cudaError_t setKernelAttributes() {
     if ((e = cudaFuncSetAttribute(kMatvecH<double, double>, A, s64))) return e;
     if ((e = cudaFuncSetAttribute(kMatvecH<float, float>, A, s32))) return e;
     if ((e = cudaFuncSetAttribute(kMatvecH<float, float, OUT_CG>, A, s32))) return e;
+    if ((e = cudaFuncSetAttribute(kMatvecH<float, float, OUT_CG_PX>, A, s32))) return e;
     if ((e = cudaFuncSetAttribute(kMatvecH<double, double, OUT_CG>, A, s64))) return e;
     if ((e = cudaFuncSetAttribute(kMatvecH<double, df, OUT_TRUE>, A, sdf))) return e;
     if ((e = cudaFuncSetAttribute(kMatvecH<double, df>, A, sdf))) return e;
@@ -1720,6 +1857,17 @@ int launchMatvec(const LaunchCtx& c, const MatvecArgs<T>& a, bool structured, co
         for (int i = 0; i < 576; ++i) k.v[i] = src[i];
         kMatvec<T><<<grid, block, smem, c.stream>>>(a, k, c.S, c.rb);
     }
+    return 1;
+}
+
+int launchMatvecPX(const LaunchCtx& c, const MatvecArgs<float>& a, const float* opconst) {
+    const Grid& g = a.g;
+    dim3 grid((g.nx + MV_TX - 2) / (MV_TX - 1), (g.ny + MV_TY - 2) / (MV_TY - 1), (g.nz + MV_ZC - 1) / MV_ZC);
+    dim3 block(MV_TX, MV_TY);
+    size_t smem = (size_t)(kSuElems + kSyElems) * sizeof(float);
+    Ks<float> k;
+    for (int i = 0; i < 45; ++i) k.v[i] = opconst[i];
+    kMatvecH<float, float, OUT_CG_PX><<<grid, block, smem, c.stream>>>(a, k, c.S, c.rb);
     return 1;
 }
 
@@ -1867,8 +2015,9 @@ int launchUpdateXR(const LaunchCtx& c, int64_t n, TX* x, TV* r, const TV* p, con
     return 1;
 }
 
-int launchFlushX(const LaunchCtx& c, int64_t n, double* x64, float* x32, const float* p, int conditional) {
-    kFlushX<<<flatBlocks(n), NT, 0, c.stream>>>(n, x64, x32, p, c.S, conditional);
+int launchFlushX(const LaunchCtx& c, int64_t n, double* x64, float* x32, const float* p, const float* pAlt,
+                 int conditional) {
+    kFlushX<<<flatBlocks(n), NT, 0, c.stream>>>(n, x64, x32, p, pAlt ? pAlt : p, c.S, conditional);
     return 1;
 }
 
@@ -1892,6 +2041,21 @@ template <typename T>
 int launchDots(const LaunchCtx& c, int64_t n, const T* a, const T* b, const T* cc, const T* d, int epi, int checkDone) {
     kDots<T><<<flatBlocks(n), NT, 0, c.stream>>>(n, a, b, cc, d, epi, c.S, c.rb, checkDone);
     return 1;
+}
+
+template <typename T>
+int launchCoarseSpace(const LaunchCtx& c, int64_t n, int k, const T* V, const T* KV, const CoarseSpace& G,
+                      const T* r, T* z, int checkDone) {
+    kCoarseDots<T><<<flatBlocks(n), NT, 0, c.stream>>>(n, k, V, KV, r, z, G, c.S, c.rb, checkDone);
+    kCoarseAxpy<T><<<flatBlocks(n), NT, 0, c.stream>>>(n, k, V, z, c.S, checkDone);
+    return 2;
+}
+
+int launchCoarseStart(const LaunchCtx& c, int64_t n, int k, const double* V, const double* KV, const CoarseSpace& G,
+                      double* x, double* r) {
+    kCoarseDots<double><<<flatBlocks(n), NT, 0, c.stream>>>(n, k, V, KV, r, nullptr, G, c.S, c.rb, 0);
+    kCoarseStart<<<flatBlocks(n), NT, 0, c.stream>>>(n, k, V, KV, c.S, x, r);
+    return 2;
 }
 
 template <typename TI, typename TO>
@@ -2044,6 +2208,7 @@ cudaError_t launchMatvecNoAlloc(cudaStream_t s, const MatvecArgs<double>& a, boo
     template int launchCoarseSolve<T>(const LaunchCtx&, CoarseInv<T>, int64_t, const int32_t*, const T*, T*, T*,    \
                                       T*, int);                                                                      \
     template int launchUpdateP<T>(const LaunchCtx&, int64_t, T*, const T*, int);                                     \
+    template int launchCoarseSpace<T>(const LaunchCtx&, int64_t, int, const T*, const T*, const CoarseSpace&, const T*, T*, int); \
     template int launchDots<T>(const LaunchCtx&, int64_t, const T*, const T*, const T*, const T*, int, int);         \
     template int launchFill<T>(cudaStream_t, int64_t, T*, T);                                                        \
     template int launchScatterCompressed<T>(cudaStream_t, int64_t, const int32_t*, const double*, T*, unsigned*);    \

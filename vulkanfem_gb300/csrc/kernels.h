@@ -38,15 +38,25 @@ struct Scalars {
     double rrTruePrev;  // true r.r of the previous replacement
     long long stalls;   // consecutive replacements without a 1% drop of the true residual
     int kernelTimeout;  // a kernel's bounded wait ran out (the solve stops with BREAKDOWN)
-    int pad2;
+    int pSel;           // fused direction update: 0 = the current p is in the first buffer, 1 = in the second
+    double coarseCoef[4];  // coarse-space coefficients G^-1 (V^T r - (KV)^T z) of the current application
+};
+
+// Deflation coarse space of k <= 4 columns V (dense storage, column j at V + j * n),
+// their products KV stored the same way, and G^-1 = (V^T K V)^-1 row-major 4 x 4.
+struct CoarseSpace {
+    double Ginv[16];
 };
 
 struct RedBuf {
-    double* partials;   // 2 * kMaxBlocks
+    double* partials;   // kMaxRedTerms * kMaxRedBlocks (term k of block b at k * kMaxRedBlocks + b)
     unsigned* ticket;
 };
 
 constexpr int kMaxRedBlocks = 1 << 16;
+// Sums one grid reduction carries at most (the partials buffer holds
+// kMaxRedTerms * kMaxRedBlocks doubles; the deflation dots use 4).
+constexpr int kMaxRedTerms = 4;
 
 // What the last block of a reducing kernel does with the totals (t0, t1).
 enum Epi : int {
@@ -87,6 +97,13 @@ struct MatvecArgs {
     int mode, dot0, dot1, epi;
     int condTrue;      // run only when a true-residual pass is due (mixed precision)
     int checkDone;
+    // Direction update fused into the FP32 CG product (launchMatvecPX): the
+    // product's input is p = z + beta p_old, with p_old in x or pAlt and the new
+    // p written to the other one (Scalars::pSel says which holds the current p),
+    // and the deferred x += alpha p_old goes into xacc.
+    const T* zin;
+    T* pAlt;
+    float* xacc;
 };
 
 struct OpConst64 { double ks[45]; double ke[576]; };
@@ -173,7 +190,12 @@ template <typename TX, typename TV>
 int launchUpdateXR(const LaunchCtx& c, int64_t n, TX* x, TV* r, const TV* p, const TV* Ap);
 // x64 += x32 (+ the deferred alpha p); x32 = 0 (mixed precision).  conditional:
 // only in iterations that recompute the FP64 true residual.
-int launchFlushX(const LaunchCtx& c, int64_t n, double* x64, float* x32, const float* p, int conditional);
+int launchFlushX(const LaunchCtx& c, int64_t n, double* x64, float* x32, const float* p, const float* pAlt,
+                 int conditional);
+// FP32 CG product with the direction update fused into its input stage
+// (structured Ke): p = z + beta p_old, x32 += alpha p_old (unless folded),
+// y = K p (fixed rows 0), p.(Kp) -> EPI_ALPHA; flips Scalars::pSel.
+int launchMatvecPX(const LaunchCtx& c, const MatvecArgs<float>& a, const float* opconst);
 // Mixed precision: r -= alpha Ap with r.r (x += alpha p deferred); p = z + beta p
 // with the deferred x += alpha p.
 int launchUpdateR(const LaunchCtx& c, int64_t n, float* r, const float* Ap);
@@ -215,6 +237,16 @@ int launchSymmetrizeLowerToFull(cudaStream_t s, T* K, int64_t n);
 // column-major upper triangle).
 template <typename T>
 int launchZeroStrictRowMajorLower(cudaStream_t s, T* K, int64_t n);
+
+// Deflated preconditioner (A-DEF2 of Tang, Nabben, Vuik and Erlangga, J. Sci.
+// Comput. 39 (2009)): z <- z + V G^-1 (V^T r - (KV)^T z) for z = M^-1 r; two
+// kernels, the 2k dots with G^-1 applied by the last block, then the update.
+template <typename T>
+int launchCoarseSpace(const LaunchCtx& c, int64_t n, int k, const T* V, const T* KV, const CoarseSpace& G,
+                      const T* r, T* z, int checkDone);
+// Start projection of deflated CG: x <- x + V mu, r <- r - KV mu, mu = G^-1 V^T r.
+int launchCoarseStart(const LaunchCtx& c, int64_t n, int k, const double* V, const double* KV, const CoarseSpace& G,
+                      double* x, double* r);
 
 // Solver scalar initialisation (device side, so it can live in a graph).
 int launchInitScalars(cudaStream_t s, Scalars* S, double tol, long long maxIter, int flexible, int mixed,

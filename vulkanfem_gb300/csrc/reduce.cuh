@@ -21,6 +21,7 @@ __device__ __forceinline__ double warpSum(double v) {
 // the last block to finish, with the totals in tot.  NTH = threads per block.
 template <int NTH, int K>
 __device__ __forceinline__ bool gridReduce(double (&v)[K], const RedBuf& rb, double (&tot)[K]) {
+    static_assert(K >= 1 && K <= kMaxRedTerms, "more sums than the partials buffer holds");
     __shared__ double sred[K][NTH / 32];
     __shared__ int amLast;
     const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);

@@ -153,12 +153,13 @@ __global__ void __launch_bounds__(128) kConvFwd(const bf16* __restrict__ in, con
 
 // Weight gradient: dW[tap][ci][co] += sum_v in[v + off(tap)][ci] * g[v][co].
 // Grid (voxel chunks, taps, ci tiles x co tiles); block 128 threads computes a
-// 64(ci) x 64(co) tile over its voxel chunk in steps of 16 voxels and adds it
-// to dW with FP32 atomics.
+// 64(ci) x 64(co) tile over its voxel chunk in steps of 16 voxels and stores it
+// in the chunk's slice of part ([chunk][27][Cin][Cout]); kWGradSum then adds
+// the chunks to dW in a fixed order, so the gradient is bit-reproducible.
 constexpr int WG_CHUNK = 2048;
 
 __global__ void __launch_bounds__(128) kConvWGrad(const bf16* __restrict__ in, const bf16* __restrict__ gout,
-                                                  float* __restrict__ dW, int n, int Cin, int Cout) {
+                                                  float* __restrict__ part, int n, int Cin, int Cout) {
     __shared__ __align__(16) bf16 sA[64][16 + 8];   // [ci][v]
     __shared__ __align__(16) bf16 sB[16][64 + 8];   // [v][co]
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -222,10 +223,19 @@ __global__ void __launch_bounds__(128) kConvWGrad(const bf16* __restrict__ in, c
         for (int hrow = 0; hrow < 2; ++hrow) {
             const int ci = ci0 + rb + g + 8 * hrow;
             const int co = co0 + 8 * j + 2 * t4;
-            float* d = dW + ((int64_t)tap * Cin + ci) * Cout + co;
-            atomicAdd(d, acc[j][2 * hrow]);
-            atomicAdd(d + 1, acc[j][2 * hrow + 1]);
+            float* d = part + (int64_t)blockIdx.x * 27 * Cin * Cout + ((int64_t)tap * Cin + ci) * Cout + co;
+            d[0] = acc[j][2 * hrow];
+            d[1] = acc[j][2 * hrow + 1];
         }
+    }
+}
+
+// dW[e] += sum over chunks c (in order) of part[c][e], e < per (= 27 Cin Cout).
+__global__ void kWGradSum(const float* __restrict__ part, float* __restrict__ dW, int64_t per, int chunks) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < per; e += (int64_t)gridDim.x * blockDim.x) {
+        float sum = 0.f;
+        for (int c = 0; c < chunks; ++c) sum += part[(int64_t)c * per + e];
+        dW[e] += sum;
     }
 }
 
@@ -412,6 +422,7 @@ struct vfem_net {
     float *ge[4] = {}, *gp[4] = {}, *gc[3] = {}, *gd[3] = {};
     bf16* gmask = nullptr;  // masked gradient scratch (largest layer)
     bf16* gbf = nullptr;    // bf16 copy of an input gradient (largest)
+    float* wgPart = nullptr;  // per-chunk weight-gradient tiles (largest layer)
     double* part = nullptr;
     float* hostStage = nullptr;
 };
@@ -479,8 +490,11 @@ void convBwd(vfem_net* N, int l, const bf16* in, const bf16* out, const float* g
     const int64_t V = N->V[lvl];
     kReluMask<<<blocks(V * Cout), 256, 0, N->stream>>>(gout, out, N->gmask, V * Cout, kRelu[l]);
     kBiasGrad<<<Cout, 256, 0, N->stream>>>(N->gmask, N->gw + N->boff[l], V, Cout);
-    dim3 gw((unsigned)((V + WG_CHUNK - 1) / WG_CHUNK), 27, (unsigned)(((Cin + 63) / 64) * ((Cout + 63) / 64)));
-    kConvWGrad<<<gw, 128, 0, N->stream>>>(in, N->gmask, N->gw + N->woff[l], n, Cin, Cout);
+    const int chunks = (int)((V + WG_CHUNK - 1) / WG_CHUNK);
+    dim3 gw((unsigned)chunks, 27, (unsigned)(((Cin + 63) / 64) * ((Cout + 63) / 64)));
+    kConvWGrad<<<gw, 128, 0, N->stream>>>(in, N->gmask, N->wgPart, n, Cin, Cout);
+    const int64_t per = 27LL * Cin * Cout;
+    kWGradSum<<<blocks(per), 256, 0, N->stream>>>(N->wgPart, N->gw + N->woff[l], per, chunks);
     if (wantIn) conv(N, N->gmask, N->wt[l], nullptr, gin, lvl, Cout, Cin, 0, true);
 }
 
@@ -571,6 +585,10 @@ vfem_status vfem_net_create(int32_t n, vfem_net** out) {
     for (int l = 0; l < kLayers; ++l) gmax = std::max<int64_t>(gmax, V[kLevel[l]] * std::max(kCin[l], kCout[l]));
     NA(nalloc(&N->gmask, gmax));
     NA(nalloc(&N->gbf, gmax));
+    int64_t wmax = 0;
+    for (int l = 0; l < kLayers; ++l)
+        wmax = std::max<int64_t>(wmax, (V[kLevel[l]] + WG_CHUNK - 1) / WG_CHUNK * 27 * kCin[l] * kCout[l]);
+    NA(nalloc(&N->wgPart, wmax));
     NA(nalloc(&N->part, 4096));
     NA(cudaMallocHost((void**)&N->hostStage, sizeof(float) * V[0] * 16));
 #undef NA
@@ -586,7 +604,7 @@ void vfem_net_destroy(vfem_net* N) {
     for (int l = 0; l < 4; ++l) { cudaFree(N->e[l]); cudaFree(N->ge[l]); cudaFree(N->p[l]); cudaFree(N->gp[l]); }
     for (int l = 0; l < 3; ++l) { cudaFree(N->c[l]); cudaFree(N->gc[l]); cudaFree(N->d[l]); cudaFree(N->gd[l]); }
     cudaFree(N->y); cudaFree(N->gy); cudaFree(N->t); cudaFree(N->mask); cudaFree(N->gmask); cudaFree(N->gbf);
-    cudaFree(N->part);
+    cudaFree(N->part); cudaFree(N->wgPart);
     if (N->hostStage) cudaFreeHost(N->hostStage);
     if (N->stream) cudaStreamDestroy(N->stream);
     delete N;

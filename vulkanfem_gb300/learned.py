@@ -209,6 +209,18 @@ def warm_start(net, d, A, f=None):
     return gamma * y
 
 
+def coarse_correction(net, d, A, f=None):
+    """The learned coarse correction: the network's predicted displacement shape
+    v becomes the deflation coarse space of A's later solves
+    (vfem_problem_set_coarse_space): PCG starts from x0 + v (v^T K v)^-1 v^T r0
+    (the warm start's energy-optimal scaling of v) and keeps every search
+    direction K-orthogonal to v.  Returns v."""
+    f = d.load_vector() if f is None else f
+    v = predict_shape(net, d, A, f)
+    A.set_coarse_space(v)
+    return v
+
+
 def predict(net, d, A=None):
     """Initial guess (compressed numbering) for domain d (needs the operator A)."""
     if A is None:

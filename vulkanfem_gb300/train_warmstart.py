@@ -4,6 +4,12 @@ evaluate what it saves on unseen domains.
     python -m vulkanfem_gb300.train_warmstart --samples 2000 --epochs 10 \
         --out vulkanfem_gb300/checkpoints/unet_warmstart.npz --eval 8 --eval-n 128
 
+Evaluation also measures the learned coarse correction (the predicted shape
+as the deflation coarse space of PCG, learned.coarse_correction; it includes
+the warm start's energy-optimal start) and, for scale, the same deflation with
+a smooth approximation of the exact solution (restricted one level and
+interpolated back: what a very good coarse-scale prediction would give).
+
 Training domains: 64^3 seeded random fields at 30-60% fill, a random load patch
 of total magnitude U[0.1, 1] in -z on the top face, z=0 fixed
 (``domains.training_field``); targets are the mixed-precision MG-PCG solutions
@@ -67,17 +73,33 @@ def evaluate(params, count, n, seed0, levels, log):
         u0 = learned.warm_start(net, d, A, f)
         t_pred = time.perf_counter() - t
         _, warm = A.solve(f, u0=u0, precision="mixed")
+        # learned coarse correction: the predicted shape as the preconditioner's coarse space
+        t = time.perf_counter()
+        learned.coarse_correction(net, d, A, f)
+        t_cc = time.perf_counter() - t
+        _, cc = A.solve(f, precision="mixed")
+        # for scale: a smooth approximation of the exact solution as the coarse space
+        A.set_coarse_space(None)
+        u_tight, _ = A.solve(f, precision="mixed", rtol=1e-10)
+        A.set_coarse_space(A.interpolate(0, A.restrict(0, u_tight)))
+        _, smooth = A.solve(f, precision="mixed")
+        A.set_coarse_space(None)
         feats = learned.domain_features(d, net.n, A, f)[0]
         net.forward(feats)
         t = time.perf_counter()
         net.forward(feats)
         t_fwd = time.perf_counter() - t
-        rows.append({"forward_ms": 1e3 * t_fwd,"cold_it": cold["iterations"], "warm_it": warm["iterations"],
+        rows.append({"forward_ms": 1e3 * t_fwd, "cold_it": cold["iterations"], "warm_it": warm["iterations"],
                      "cold_ms": cold["solve_ms"], "warm_ms": warm["solve_ms"], "predict_ms": 1e3 * t_pred,
-                     "cold_relres": cold["rel_residual"], "warm_relres": warm["rel_residual"]})
+                     "coarse_it": cc["iterations"], "coarse_ms": cc["solve_ms"], "coarse_setup_ms": 1e3 * t_cc,
+                     "smooth_coarse_it": smooth["iterations"], "smooth_coarse_ms": smooth["solve_ms"],
+                     "cold_relres": cold["rel_residual"], "warm_relres": warm["rel_residual"],
+                     "coarse_relres": cc["rel_residual"], "smooth_coarse_relres": smooth["rel_residual"]})
         A.close()
-        log("eval %d: cold %d it %.1f ms, warm %d it %.1f ms (+%.1f ms predict)" % (
-            i, cold["iterations"], cold["solve_ms"], warm["iterations"], warm["solve_ms"], 1e3 * t_pred))
+        log("eval %d: cold %d it %.1f ms, warm %d it %.1f ms (+%.1f ms predict), learned coarse %d it %.1f ms, "
+            "smoothed-solution coarse space %d it %.1f ms" % (
+                i, cold["iterations"], cold["solve_ms"], warm["iterations"], warm["solve_ms"], 1e3 * t_pred,
+                cc["iterations"], cc["solve_ms"], smooth["iterations"], smooth["solve_ms"]))
     net.close()
     return rows
 
@@ -128,7 +150,12 @@ def main(argv=None):
         "mean_warm_iterations": float(np.mean([r["warm_it"] for r in rows])),
         "mean_cold_ms": float(np.mean([r["cold_ms"] for r in rows])),
         "mean_warm_ms_incl_predict": float(np.mean([r["warm_ms"] + r["predict_ms"] for r in rows])),
+        "mean_coarse_iterations": float(np.mean([r["coarse_it"] for r in rows])),
+        "mean_coarse_ms_incl_setup": float(np.mean([r["coarse_ms"] + r["coarse_setup_ms"] for r in rows])),
+        "mean_smooth_coarse_iterations": float(np.mean([r["smooth_coarse_it"] for r in rows])),
+        "mean_smooth_coarse_ms": float(np.mean([r["smooth_coarse_ms"] for r in rows])),
         "max_warm_relres": float(max(r["warm_relres"] for r in rows)),
+        "max_coarse_relres": float(max(max(r["coarse_relres"], r["smooth_coarse_relres"]) for r in rows)),
         "rows": rows,
     }
     print(json.dumps(summary), flush=True)
