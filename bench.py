@@ -268,6 +268,8 @@ def main():
     ap.add_argument("--cpu-iters", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-reps", type=int, default=20)
+    ap.add_argument("--no-extra-configs", action="store_true",
+                    help="skip the 128^3 porous FP32-vs-FP64 pair added to the line")
     ap.add_argument("--kernels-only", action="store_true",
                     help="profiling case for ncu: set-up, a 4-iteration solve and one launch of each kernel class; "
                          "prints the kernel-class times and no bench line")
@@ -322,12 +324,12 @@ def main():
     # ---- end to end through the C ABI with host buffers (e2e)
     f = dom.load_vector()
     u = np.empty(dof)
-    A.solve(f, **sopts)
+    A.solve(f, out=u, **sopts)  # (the caller's output array is reused, as a C caller's would be)
     dist.barrier()
     e_it = 0
     e0 = time.perf_counter()
     for _ in range(args.steps):
-        u, st = A.solve(f, **sopts)
+        u, st = A.solve(f, out=u, **sopts)
         e_it += st["iterations"]
     e_s = time.perf_counter() - e0
     e2e, _ = replica_throughput(dist, e_s, dof * e_it)
@@ -408,6 +410,9 @@ def main():
         "roofline": roof,
         "clocks": clk.summary(),
     }
+    if rank == 0 and ws == 1 and not args.no_extra_configs:
+        A.close()
+        line["configs"] = {"porous128": precision_pair("porous128", args.steps)}
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args, dom)
         line["cpu_baseline_serial"] = cpu_baseline(args, dom, threads=1, iters=1)
@@ -417,6 +422,31 @@ def main():
         print(json.dumps(line), flush=True)
     A.close()
     dist.close()
+
+
+def precision_pair(workload, steps):
+    """The FP32-vs-FP64 configuration on a second workload: both solvers timed
+    device-resident to rtol 1e-6 on the same problem, with the relative L2
+    difference of their answers."""
+    from vulkanfem_gb300 import api, domains
+    dom = WORKLOADS[workload][0]()
+    A = api.assembleSystemMatrix(dom.voxels, domains.hex8_stiffness(), dom.fixed, dom.num_levels, 0, E=dom.E)
+    A.set_loads(dom.load_nodes, dom.load_values)
+    dof = A.rows()
+    out = {"description": WORKLOADS[workload][1], "dofs": dof}
+    u = {}
+    for name in ("mixed", "fp64"):
+        A.solve_device(**SOLVERS[name])
+        sts = [A.solve_device(**SOLVERS[name])[1] for _ in range(max(1, min(steps, 3)))]
+        t = sum(st["solve_ms"] for st in sts) / len(sts) / 1e3
+        it = sum(st["iterations"] for st in sts) / len(sts)
+        u[name], _ = A.solve_device(want_solution=True, **SOLVERS[name])
+        out[name] = {"time_to_rtol_s": t, "iterations": it, "mdof_s": dof * it / t / 1e6,
+                     "rel_residual": sts[-1]["rel_residual"]}
+    out["speedup_time_to_rtol"] = out["fp64"]["time_to_rtol_s"] / out["mixed"]["time_to_rtol_s"]
+    out["rel_l2_mixed_vs_fp64"] = float(np.linalg.norm(u["mixed"] - u["fp64"]) / np.linalg.norm(u["fp64"]))
+    A.close()
+    return out
 
 
 if __name__ == "__main__":

@@ -343,12 +343,18 @@ class MatrixFreeSparse:
             raise VfemError(1, "vector size mismatch")
         _check(self._lib.vfem_problem_set_rhs(self._h, f))
 
-    def solve(self, f=None, u0=None, allow_not_converged=False, **opts):
-        """Solve K u = f (f defaults to the loads already set).  Returns (u, stats)."""
+    def solve(self, f=None, u0=None, allow_not_converged=False, out=None, **opts):
+        """Solve K u = f (f defaults to the loads already set).  Returns (u, stats);
+        u is ``out`` when given (a C-contiguous float64 array of ``rows()``)."""
         if f is not None:
             self.set_rhs(f)
         o = make_options(**opts)
-        u = np.empty(self.rows(), np.float64)
+        if out is None:
+            u = np.empty(self.rows(), np.float64)
+        else:
+            u = out
+            if u.dtype != np.float64 or u.size != self.rows() or not u.flags.c_contiguous:
+                raise VfemError(1, "out must be a C-contiguous float64 array of rows() values")
         st = Stats()
         u0p = None
         if u0 is not None:

@@ -1209,14 +1209,12 @@ vfem_status solveImpl(vfem_problem* p, const vfem_options* optIn, bool haveX0, v
     return s;
 }
 
-// Host compressed vector -> dense device vector of level lv.  checkFinite: the
-// scatter flags non-finite input (read back by the caller after a sync).
 // memcpy split over host threads for large host <-> pinned copies (one thread
 // copies ~10 GB/s on the Grace host; the staging copies are 8 bytes per DOF).
 void hostCopy(void* dst, const void* src, size_t bytes) {
     const size_t kSlice = (size_t)32 << 20;
     const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-    const size_t nt = std::min<size_t>({(size_t)8, (size_t)hw, (bytes + kSlice - 1) / kSlice});
+    const size_t nt = std::min<size_t>({(size_t)16, (size_t)hw, (bytes + kSlice - 1) / kSlice});
     if (nt <= 1) {
         std::memcpy(dst, src, bytes);
         return;

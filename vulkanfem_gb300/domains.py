@@ -190,7 +190,8 @@ def spheres(n=256, count=300, rmin=4.0, rmax=16.0, seed=0, levels=5, lognormal_s
 
 def training_field(n=64, seed=0, levels=3):
     """A training domain: fill U[0.30, 0.60], a random axis-aligned load patch
-    on the top face with total magnitude U[0.1, 1] in -z, z=0 fixed."""
+    on the top face with total magnitude U[0.1, 1] in -z, z=0 fixed.  Raises
+    ValueError when no filled voxel of the field is connected to z = 0."""
     from scipy import ndimage
     rng = np.random.default_rng(seed)
     fill = rng.uniform(0.30, 0.60)
@@ -214,6 +215,8 @@ def training_field(n=64, seed=0, levels=3):
     else:
         sel = plane[plane >= 0]
     ln = np.sort(sel.reshape(-1))
+    if ln.size == 0:
+        raise ValueError("training field %d (seed %d): no filled voxel is connected to z = 0" % (n, seed))
     lv = np.zeros((ln.size, 3))
     lv[:, 2] = -mag / ln.size
     return Domain("train_%d_s%d" % (n, seed), vox, fixed, ln, lv, None, levels, seed,

@@ -27,6 +27,10 @@ import numpy as np
 from . import api, domains, learned
 
 NF = 9  # feature channels in use (see learned.py)
+# Iteration caps: a field whose solve does not converge within them (floppy
+# parts barely attached to the fixed face) is replaced by the next seed.
+DATA_MAX_ITER = 5000
+EVAL_MAX_ITER = 10000
 
 def build_dataset(count, n, seed0, levels, log):
     ke = domains.hex8_stiffness()
@@ -36,11 +40,25 @@ def build_dataset(count, n, seed0, levels, log):
     M = np.zeros((count, npad, npad, npad), np.uint8)
     t0 = time.time()
     its = []
+    seed, skipped = seed0, 0
     for i in range(count):
-        d = domains.training_field(n, seed=seed0 + i, levels=levels)
-        A = api.assembleSystemMatrix(d.voxels, ke, d.fixed, levels)
-        f = d.load_vector()
-        u, st = A.solve(f, precision="mixed")
+        while True:
+            # a field whose grounded part is tiny gets Eigen's small default cap
+            # (2 x DOFs) and may not converge within it: take the next seed
+            try:
+                d = domains.training_field(n, seed=seed, levels=levels)
+            except ValueError:  # nothing connected to the fixed face
+                seed += 1
+                skipped += 1
+                continue
+            seed += 1
+            A = api.assembleSystemMatrix(d.voxels, ke, d.fixed, levels)
+            f = d.load_vector()
+            u, st = A.solve(f, precision="mixed", max_iter=DATA_MAX_ITER, allow_not_converged=True)
+            if st["status"] == 0:
+                break
+            A.close()
+            skipped += 1
         its.append(st["iterations"])
         feats, mask, scale = learned.domain_features(d, npad, A, f)
         A.close()
@@ -48,7 +66,8 @@ def build_dataset(count, n, seed0, levels, log):
         T[i] = learned.target_grid(u, mask, scale, npad)
         M[i] = learned.loss_mask(mask, d.fixed, npad) > 0
         if (i + 1) % 100 == 0:
-            log("data %d/%d  %.0f s  mean iterations %.1f" % (i + 1, count, time.time() - t0, np.mean(its)))
+            log("data %d/%d  %.0f s  mean iterations %.1f  (%d fields skipped: empty or not converged)"
+                % (i + 1, count, time.time() - t0, np.mean(its), skipped))
     return F, T, M
 
 
@@ -63,26 +82,37 @@ def evaluate(params, count, n, seed0, levels, log):
     ke = domains.hex8_stiffness()
     net = learned.UNet(learned.padded(n + 1), params)
     rows = []
-    for i in range(count):
-        d = domains.training_field(n, seed=seed0 + i, levels=levels)
+    seed = seed0
+    while len(rows) < count:
+        try:
+            d = domains.training_field(n, seed=seed, levels=levels)
+        except ValueError:  # nothing connected to the fixed face
+            seed += 1
+            continue
+        seed += 1
         A = api.assembleSystemMatrix(d.voxels, ke, d.fixed, levels)
         f = d.load_vector()
-        A.solve(f, precision="mixed")  # graph capture outside the timing
-        _, cold = A.solve(f, precision="mixed")
+        _, st = A.solve(f, precision="mixed", max_iter=EVAL_MAX_ITER,
+                        allow_not_converged=True)  # graph capture outside the timing
+        if st["status"] != 0:  # not converged within the default cap: next field
+            A.close()
+            continue
+        i = len(rows)
+        _, cold = A.solve(f, precision="mixed", max_iter=EVAL_MAX_ITER)
         t = time.perf_counter()
         u0 = learned.warm_start(net, d, A, f)
         t_pred = time.perf_counter() - t
-        _, warm = A.solve(f, u0=u0, precision="mixed")
+        _, warm = A.solve(f, u0=u0, precision="mixed", max_iter=EVAL_MAX_ITER, allow_not_converged=True)
         # learned coarse correction: the predicted shape as the preconditioner's coarse space
         t = time.perf_counter()
         learned.coarse_correction(net, d, A, f)
         t_cc = time.perf_counter() - t
-        _, cc = A.solve(f, precision="mixed")
+        _, cc = A.solve(f, precision="mixed", max_iter=EVAL_MAX_ITER, allow_not_converged=True)
         # for scale: a smooth approximation of the exact solution as the coarse space
         A.set_coarse_space(None)
-        u_tight, _ = A.solve(f, precision="mixed", rtol=1e-10)
+        u_tight, _ = A.solve(f, precision="mixed", rtol=1e-10, max_iter=4 * EVAL_MAX_ITER, allow_not_converged=True)
         A.set_coarse_space(A.interpolate(0, A.restrict(0, u_tight)))
-        _, smooth = A.solve(f, precision="mixed")
+        _, smooth = A.solve(f, precision="mixed", max_iter=EVAL_MAX_ITER, allow_not_converged=True)
         A.set_coarse_space(None)
         feats = learned.domain_features(d, net.n, A, f)[0]
         net.forward(feats)
