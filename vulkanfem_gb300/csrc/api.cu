@@ -1214,7 +1214,8 @@ vfem_status solveImpl(vfem_problem* p, const vfem_options* optIn, bool haveX0, v
 void hostCopy(void* dst, const void* src, size_t bytes) {
     const size_t kSlice = (size_t)32 << 20;
     const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-    const size_t nt = std::min<size_t>({(size_t)16, (size_t)hw, (bytes + kSlice - 1) / kSlice});
+    static const size_t cap = (size_t)std::max<long long>(1, envInt("VFEM_HOST_COPY_THREADS", 8));
+    const size_t nt = std::min<size_t>({cap, (size_t)hw, (bytes + kSlice - 1) / kSlice});
     if (nt <= 1) {
         std::memcpy(dst, src, bytes);
         return;

@@ -107,11 +107,13 @@ def evaluate(params, count, n, seed0, levels, log):
         t = time.perf_counter()
         learned.coarse_correction(net, d, A, f)
         t_cc = time.perf_counter() - t
+        A.solve(f, precision="mixed", max_iter=EVAL_MAX_ITER, allow_not_converged=True)  # graph capture
         _, cc = A.solve(f, precision="mixed", max_iter=EVAL_MAX_ITER, allow_not_converged=True)
         # for scale: a smooth approximation of the exact solution as the coarse space
         A.set_coarse_space(None)
         u_tight, _ = A.solve(f, precision="mixed", rtol=1e-10, max_iter=4 * EVAL_MAX_ITER, allow_not_converged=True)
         A.set_coarse_space(A.interpolate(0, A.restrict(0, u_tight)))
+        A.solve(f, precision="mixed", max_iter=EVAL_MAX_ITER, allow_not_converged=True)  # graph capture
         _, smooth = A.solve(f, precision="mixed", max_iter=EVAL_MAX_ITER, allow_not_converged=True)
         A.set_coarse_space(None)
         feats = learned.domain_features(d, net.n, A, f)[0]
@@ -134,6 +136,28 @@ def evaluate(params, count, n, seed0, levels, log):
     return rows
 
 
+def summarize(rows):
+    """Means over the evaluated fields (iterations, times including the
+    prediction or the coarse-space set-up, largest relative residuals)."""
+    mean = lambda key: float(np.mean([r[key] for r in rows]))
+    return {
+        "eval_count": len(rows),
+        "mean_cold_iterations": mean("cold_it"),
+        "mean_warm_iterations": mean("warm_it"),
+        "mean_coarse_iterations": mean("coarse_it"),
+        "mean_smooth_coarse_iterations": mean("smooth_coarse_it"),
+        "mean_cold_ms": mean("cold_ms"),
+        "mean_warm_ms": mean("warm_ms"),
+        "mean_predict_ms": mean("predict_ms"),
+        "mean_coarse_ms": mean("coarse_ms"),
+        "mean_coarse_setup_ms": mean("coarse_setup_ms"),
+        "mean_smooth_coarse_ms": mean("smooth_coarse_ms"),
+        "mean_forward_ms": mean("forward_ms"),
+        "max_warm_relres": float(max(r["warm_relres"] for r in rows)),
+        "max_coarse_relres": float(max(max(r["coarse_relres"], r["smooth_coarse_relres"]) for r in rows)),
+    }
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--samples", type=int, default=2000)
@@ -146,8 +170,14 @@ def main(argv=None):
     ap.add_argument("--eval", type=int, default=8)
     ap.add_argument("--eval-n", type=int, default=128)
     ap.add_argument("--eval-levels", type=int, default=5)
+    ap.add_argument("--eval-only", default=None, metavar="CHECKPOINT",
+                    help="evaluate a saved checkpoint instead of training")
     args = ap.parse_args(argv)
     log = lambda s: print(s, file=sys.stderr, flush=True)
+    if args.eval_only:
+        rows = evaluate(learned.load(args.eval_only), args.eval, args.eval_n, 1_000_000, args.eval_levels, log)
+        print(json.dumps(dict(summarize(rows), checkpoint=args.eval_only, rows=rows)), flush=True)
+        return
     t0 = time.time()
     F, T, M = build_dataset(args.samples, args.n, 0, args.levels, log)
     t_data = time.time() - t0
@@ -172,22 +202,9 @@ def main(argv=None):
     learned.save(args.out, params, {"samples": args.samples, "epochs": args.epochs, "n": args.n,
                                      "loss_history": np.asarray(hist)})
     rows = evaluate(learned.load(args.out), args.eval, args.eval_n, 1_000_000, args.eval_levels, log)
-    summary = {
-        "samples": args.samples, "n": args.n, "epochs": args.epochs, "data_s": t_data, "train_s": t_train,
-        "loss_history": hist,
-        "eval_n": args.eval_n, "eval_count": len(rows),
-        "mean_cold_iterations": float(np.mean([r["cold_it"] for r in rows])),
-        "mean_warm_iterations": float(np.mean([r["warm_it"] for r in rows])),
-        "mean_cold_ms": float(np.mean([r["cold_ms"] for r in rows])),
-        "mean_warm_ms_incl_predict": float(np.mean([r["warm_ms"] + r["predict_ms"] for r in rows])),
-        "mean_coarse_iterations": float(np.mean([r["coarse_it"] for r in rows])),
-        "mean_coarse_ms_incl_setup": float(np.mean([r["coarse_ms"] + r["coarse_setup_ms"] for r in rows])),
-        "mean_smooth_coarse_iterations": float(np.mean([r["smooth_coarse_it"] for r in rows])),
-        "mean_smooth_coarse_ms": float(np.mean([r["smooth_coarse_ms"] for r in rows])),
-        "max_warm_relres": float(max(r["warm_relres"] for r in rows)),
-        "max_coarse_relres": float(max(max(r["coarse_relres"], r["smooth_coarse_relres"]) for r in rows)),
-        "rows": rows,
-    }
+    summary = dict({"samples": args.samples, "n": args.n, "epochs": args.epochs, "data_s": t_data,
+                    "train_s": t_train, "loss_history": hist}, **summarize(rows))
+    summary["rows"] = rows
     print(json.dumps(summary), flush=True)
 
 
