@@ -127,11 +127,17 @@ def test_coarse_space_deflation_mechanism():
         assert st2["iterations"] <= base["iterations"] + 1, (prec, base["iterations"], st2["iterations"])
         print("%s: %d iterations, %d with the smoothed solution as coarse space" % (prec, base["iterations"],
                                                                                  st2["iterations"]))
-    # two columns (smoothed solution, load direction) and removal
+    # two columns (smoothed solution, load direction), also in flexible CG
+    # (Polak-Ribiere beta, which tolerates the A-DEF2 operator's rounding
+    # asymmetry), and removal
     A.set_coarse_space(np.stack([u_smooth, f], 1))
     u3, st3 = A.solve(f)
     assert st3["rel_residual"] < 1e-6 and _rel(u3, u0) < 1e-5
     assert st3["iterations"] <= st0["iterations"] + 1
+    for prec in ("fp64", "mixed"):
+        u5, st5 = A.solve(f, precision=prec, flexible=True)
+        assert st5["rel_residual"] < 1e-6 and st5["fallback"] == 0 and _rel(u5, u0) < 1e-5
+        assert st5["iterations"] <= st0["iterations"] + 2, (prec, st0["iterations"], st5["iterations"])
     A.set_coarse_space(None)
     _, st4 = A.solve(f)
     assert st4["iterations"] == st0["iterations"]
@@ -169,9 +175,12 @@ def test_learned_coarse_correction_reaches_the_same_answer(trained):
         uc, cold = A.solve(f, precision="mixed")
         learned.coarse_correction(net, d, A, f)
         ul, lc = A.solve(f, precision="mixed")
+        uf, lf = A.solve(f, precision="mixed", flexible=True)  # inside flexible PCG
         A.close()
         assert lc["rel_residual"] < 1e-6 and lc["fallback"] == 0
-        assert _rel(ul, uc) < 1e-5
+        assert lf["rel_residual"] < 1e-6 and lf["fallback"] == 0
+        assert _rel(ul, uc) < 1e-5 and _rel(uf, uc) < 1e-5
         assert lc["iterations"] <= 1.10 * cold["iterations"] + 2, (cold["iterations"], lc["iterations"])
-        print("field %d: %d iterations plain, %d with the learned coarse correction"
-              % (seed, cold["iterations"], lc["iterations"]))
+        assert lf["iterations"] <= 1.10 * cold["iterations"] + 2, (cold["iterations"], lf["iterations"])
+        print("field %d: %d iterations plain, %d with the learned coarse correction (%d in flexible PCG)"
+              % (seed, cold["iterations"], lc["iterations"], lf["iterations"]))
