@@ -283,3 +283,30 @@ def test_rhs_checks_and_host_transfers(case):
     A.set_rhs(f)
     ud, std = A.solve_device(want_solution=True, precision="mixed")
     assert np.array_equal(u, ud) and st["iterations"] == std["iterations"]
+
+
+def test_patch_test_known_answers_gpu():
+    """Analytic known answers through the C ABI (tests/patch_test.py), on a
+    40 x 12 x 40 solid box that spans several product blocks in x, y and z:
+    the FP64 product of a linear field equals the consistent traction loads
+    to 1e-12 of the largest load (zero at interior nodes); the FP32 product
+    to 2e-5 of max|u| (its rounding is relative to the terms K u, about 30x
+    the loads here); the FP64 and mixed solves with those loads return the
+    linear field (1e-8 at rtol 1e-12; 1e-5 at rtol 1e-9)."""
+    from tests import patch_test as pt
+    vox, fixed, coords = pt.box(40, 12, 40)
+    A = api.assembleSystemMatrix(vox, domains.hex8_stiffness(pt.E, pt.NU), fixed, 3, 0)
+    for name, u, f in pt.fields(vox, coords):
+        g = pt.expected_product(f, fixed)
+        scale = np.max(np.abs(g))
+        assert np.max(np.abs(A @ u - g)) < 1e-12 * scale, name
+        y32, _ = A.dot_mixed(u)
+        assert np.max(np.abs(y32 - g)) < 2e-5 * np.max(np.abs(u)), name
+        x, st = A.solve(g, rtol=1e-12)
+        assert rel(x, u) < 1e-8, (name, st["iterations"], rel(x, u))
+        xm, stm = A.solve(g, precision="mixed", rtol=1e-9)
+        assert stm["rel_residual"] < 1e-9 and stm["fallback"] == 0
+        assert rel(xm, u) < 1e-5, (name, rel(xm, u))
+        print("patch test %s: FP64 product %.1e, FP32 %.1e of the largest load; solves %.1e (fp64), %.1e (mixed)"
+              % (name, np.max(np.abs(A @ u - g)) / scale, np.max(np.abs(y32 - g)) / scale, rel(x, u), rel(xm, u)))
+    A.close()

@@ -190,3 +190,19 @@ def test_armadillo_hierarchy(armadillo):
     assert o.num_dofs(0) == 562455
     assert o.num_levels == 3
     assert o.level_dims(1) == (56, 64, 64) and o.level_dims(2) == (28, 32, 32)
+
+
+def test_patch_test_known_answers():
+    """Analytic known answers (tests/patch_test.py): the oracle's product of a
+    linear field on a solid box is zero inside and the consistent traction
+    loads on the faces (to 1e-12 of the largest load), and its MG-PCG solve
+    with those loads returns the linear field (to 1e-9 at rtol 1e-12)."""
+    from tests import patch_test as pt
+    vox, fixed, coords = pt.box()
+    o = oracle.Oracle(vox, domains.hex8_stiffness(pt.E, pt.NU), fixed, 2, 0)
+    for name, u, f in pt.fields(vox, coords):
+        g = pt.expected_product(f, fixed)
+        y = o.matvec(u)
+        assert np.max(np.abs(y - g)) < 1e-12 * np.max(np.abs(g)), name
+        x, it, _ = o.pcg(g, tol=1e-12)
+        assert np.linalg.norm(x - u) < 1e-9 * np.linalg.norm(u), (name, it)
