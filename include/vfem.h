@@ -122,7 +122,11 @@ vfem_status vfem_hex8_stiffness(double E, double nu, double* Ke_out);
 /* assembleSystemMatrix<double>(voxels, dims, Ke, fixedNodes, numLevels, skipLevels)
  * (include/FEM.hpp:33-34).  E_or_null: per-voxel Young's modulus multiplier
  * (same layout as voxels) or NULL for a uniform 1.  fixed_nodes: compressed node
- * ids (0-based).  num_levels >= 1; skip_levels in {0, 1} (4x first coarsening,
+ * ids (0-based); at least one is required (VFEM_ERR_INVALID_ARGUMENT otherwise:
+ * without fixed nodes the stiffness is singular through its rigid-body modes,
+ * which the reference does not check).  Every connected component of the
+ * voxels must contain a fixed node for the same reason; that is not checked.
+ * num_levels >= 1; skip_levels in {0, 1} (4x first coarsening,
  * FEM.cpp:266-272).  The hierarchy stops early when a dimension reaches <= 2
  * elements (FEM.cpp:465-470). */
 vfem_status vfem_problem_create(const uint8_t* voxels, int32_t nx, int32_t ny, int32_t nz,

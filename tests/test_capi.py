@@ -71,3 +71,16 @@ def test_create_reports_errors_instead_of_aborting():
     fixed = np.array([0], np.int64)
     s = lib.vfem_problem_create(vox.reshape(-1), 2, 2, 2, ke, None, fixed, 1, 0, 0, ctypes.byref(h))
     assert s != 0 and not h.value
+
+
+def test_create_rejects_an_empty_fixed_set():
+    """Without fixed nodes the stiffness is singular (rigid-body modes): the
+    set-up refuses with VFEM_ERR_INVALID_ARGUMENT before touching the device."""
+    lib = api.load_library()
+    vox = np.ones((2, 2, 2), np.uint8)
+    ke = np.ascontiguousarray(domains.hex8_stiffness().reshape(-1))
+    h = ctypes.c_void_p()
+    fixed = np.zeros(1, np.int64)
+    s = lib.vfem_problem_create(vox.reshape(-1), 2, 2, 2, ke, None, fixed, 0, 2, 0, ctypes.byref(h))
+    assert s == 1 and not h.value
+    assert b"fixed" in lib.vfem_last_error_message()

@@ -240,7 +240,9 @@ def test_per_voxel_modulus():
 
 def test_setup_rejects_bad_input_with_status_codes():
     """The device set-up reports invalid input as status codes and leaves the
-    library usable (VFEM_ERR_INVALID_ARGUMENT = 1, VFEM_ERR_EMPTY = 7)."""
+    library usable (VFEM_ERR_INVALID_ARGUMENT = 1, VFEM_ERR_EMPTY = 7): voxel
+    values other than 0/1, non-positive or non-finite moduli, an empty domain,
+    an out-of-range fixed id, no fixed node at all."""
     import ctypes
     lib = api.load_library()
     ke = np.ascontiguousarray(domains.hex8_stiffness().reshape(-1))
@@ -266,6 +268,7 @@ def test_setup_rejects_bad_input_with_status_codes():
     assert create(vox, E) == 1
     assert create(np.zeros_like(vox)) == 7
     assert create(vox, fx=np.array([10 ** 6], np.int64)) == 1
+    assert create(vox, fx=np.zeros(0, np.int64)) == 1  # no fixed nodes: singular stiffness
     assert create(vox) == 0
 
 

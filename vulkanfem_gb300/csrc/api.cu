@@ -661,12 +661,17 @@ vfem_status createImpl(const uint8_t* vox, int nx, int ny, int nz, const double*
                        const int64_t* fixed, int64_t nfixed, int numLevels, int skip, vfem_problem** out) {
     if (!vox || !Ke || !out || (nfixed > 0 && !fixed))
         return fail(VFEM_ERR_INVALID_ARGUMENT, "null pointer argument");
+    if (nfixed <= 0)
+        return fail(VFEM_ERR_INVALID_ARGUMENT, "no fixed nodes: the stiffness would be singular (rigid-body modes)");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(VFEM_ERR_NO_DEVICE, "no CUDA device");
     g_coarse64Min = std::max<long long>(1, envInt("VFEM_COARSE_64BIT_MIN", kMaxCoarse32));
     g_allocCountdown = std::max<long long>(0, envInt("VFEM_FAULT_ALLOC_AT", 0));
     vfem_problem* p = new vfem_problem();
-    CK(cudaGetDevice(&p->device));
+    if (cudaGetDevice(&p->device) != cudaSuccess) {
+        delete p;
+        return fail(VFEM_ERR_CUDA, "cudaGetDevice");
+    }
     vfem_status st = prepareKe(Ke, p->ke);
     if (st != VFEM_OK) {
         delete p;
