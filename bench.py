@@ -177,7 +177,7 @@ def algorithmic_bytes(kind, g0, g1, s):
     """Algorithmic bytes per launch on the finest level.  N = grid nodes, Ne = voxels
     (dense-grid model): matvec 6sN + Ne/8 + 4Ne + N/8 (x in, y out, occupancy bits,
     modulus, fixed bits); restrict 3sN_f + 3sN_c; prolong+smooth 3sN_c + 9sN_f (z_c,
-    r, D^-1 in; z out) + N_f/8; x/r update 18sN (x, r, p, Ap in; x, r out); p
+    r, D^-1 in; z out) + N_f/8, 7.5sN_f in the mixed solve (D^-1 in FP16); x/r update 18sN (x, r, p, Ap in; x, r out); p
     update 9sN.  The mixed solve defers x += alpha p (its FP32 x correction) to
     the p update: r update 9sN, p update 15sN (z, p, x in; p, x out).  With the
     p update fused into the product (matvec_px): p_old, z, x in and p, x, Kp out
@@ -188,10 +188,15 @@ def algorithmic_bytes(kind, g0, g1, s):
         return 6 * s * N + Ne / 8 + 4 * Ne + N / 8
     if kind == "matvec_px":
         return 18 * s * N + Ne / 8 + 4 * Ne + N / 8
+    if kind == "update_restrict":  # r, Ap in and the new r out on the fine level; the coarse r out
+        return 9 * s * N + 3 * s * Nc
+    if kind == "coarse":  # the coarsest dense inverse: FP16 lower block triangle (mixed) or FP64 full
+        n = g1["coarse_free"]
+        return n * n if s == 4 else 8 * n * n
     if kind == "restrict":
         return 3 * s * N + 3 * s * Nc
-    if kind == "prolong":
-        return 3 * s * Nc + 9 * s * N + N / 8
+    if kind == "prolong":  # the mixed up-leg reads D^-1 in FP16 (6 instead of 12 bytes per node)
+        return 3 * s * Nc + (7.5 if s == 4 else 9) * s * N + N / 8
     if kind == "update_xr":
         return (9 if s == 4 else 18) * s * N
     if kind == "update_p":
@@ -354,16 +359,20 @@ def main():
     ms = api.profile_kernels(A, args.profile_reps)
     g0 = {"nodes": int(np.prod([n + 1 for n in dom.voxels.shape])), "voxels": int(dom.voxels.size)}
     sh1 = [-(-n // 2) + 1 for n in dom.voxels.shape]
-    g1 = {"nodes": int(np.prod(sh1))}
+    g1 = {"nodes": int(np.prod(sh1)), "coarse_free": int(A.coarse_free_dofs)}
     mixed = sopts["precision"] == "mixed"
     s = 4 if mixed else 8
-    per_iter = {  # kernel class -> (ms, launches per iteration, bytes kind)
+    per_iter = {  # finest-level kernel class the solve runs once per iteration -> (ms, launches)
         "matvec": (ms["matvec_fp32" if mixed else "matvec_fp64"], 1),
         "update_xr": (ms["update_xr_mixed" if mixed else "update_xr_fp64"], 1),
         "prolong": (ms["prolong_fp32" if mixed else "prolong_fp64"], 1),
         "restrict": (ms["restrict_fp32" if mixed else "restrict_fp64"], 1),
         "update_p": (ms["update_p_fp32" if mixed else "update_p_fp64"], 1),
+        "coarse": (ms["coarse_fp32" if mixed else "coarse_fp64"], 1),
     }
+    if mixed and ms.get("update_restrict_mixed", 0) > 0:  # residual update fused with the first restriction
+        per_iter["update_restrict"] = (ms["update_restrict_mixed"], 1)
+        del per_iter["update_xr"], per_iter["restrict"]
     if mixed and ms.get("matvec_fp32_px", 0) > 0:  # the solve runs the fused product instead
         per_iter["matvec_px"] = (ms["matvec_fp32_px"], 1)
         del per_iter["matvec"], per_iter["update_p"]
@@ -379,10 +388,16 @@ def main():
             tt = json.load(fh)
         key = "%s/%s_%s" % (args.workload, dom_k, "fp32" if mixed else "fp64")
         traffic = tt.get(key)
+    per_kernel = {}
+    for k, (kt, _) in per_iter.items():
+        b = algorithmic_bytes(k, g0, g1, s)
+        per_kernel["%s_%s" % (k, "fp32" if mixed else "fp64")] = {
+            "ms_per_launch": kt, "algorithmic_bytes": b, "achieved_gbs": b / (kt * 1e-3) / 1e9 if kt > 0 else None,
+            "frac": b / (kt * 1e-3) / 1e9 / peak if kt > 0 else None}
     roof = {"kernel": "%s_%s" % (dom_k, "fp32" if mixed else "fp64"), "bound": "hbm", "achieved": achieved,
             "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
             "algorithmic_bytes": abytes, "ms_per_launch": kms, "peak_source": peak_src,
-            "kernel_ms": ms}
+            "per_kernel": per_kernel, "kernel_ms": ms}
 
     o_full = api.make_options(**sopts)
     solver_options = {k: getattr(o_full, k) for k, _ in api.Options._fields_ if k != "reserved"}
