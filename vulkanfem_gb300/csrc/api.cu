@@ -1197,9 +1197,18 @@ vfem_status solveImpl(vfem_problem* p, const vfem_options* optIn, bool haveX0, v
     o2.precision = VFEM_PREC_FP64;
     o2.max_iter = budget - s1.iterations;
     o2.debug_break_at = 0;
+    o2.compute_true_residual = 1;
     vfem_stats s2;
     std::memset(&s2, 0, sizeof(s2));
-    s = solvePhase(p, o2, std::isfinite(s1.rel_residual), &s2);
+    // The FP64 solve continues from the mixed iterate only when that is better
+    // than zero (true relative residual below 1); a diverged iterate would
+    // leave the recursive residual far from the true one.
+    const bool fromIterate = std::isfinite(s1.rel_residual) && s1.rel_residual < 1.0;
+    s = solvePhase(p, o2, fromIterate, &s2);
+    // The recursive residual of the continued solve decides convergence as in
+    // Eigen; the fallback also requires the true residual near the tolerance.
+    if (s == VFEM_OK && !(s2.rel_residual <= 10.0 * o.rtol))
+        s = fail(VFEM_ERR_NOT_CONVERGED, "FP64 fallback: true residual above 10 x rtol");
     if (st) {
         *st = s2;
         st->iterations = s1.iterations + s2.iterations;
