@@ -12,7 +12,7 @@
 //   kProlongFlat, kProlongSmooth2, kProlongSmooth  Interpolate.comp + PreSmoothAndAXPY.comp +
 //                    Smooth.comp (MultigridPreconditioner.hpp:110-155,176-181),
 //                    fixed mask and r.z fused.
-//   kCoarseGather/kSymTile/kSymReduce, kGemv64  the coarsest SimplicialLDLT solve
+//   kCoarseGather/kSymRuns/kSymRunsReduce, kGemv64  the coarsest SimplicialLDLT solve
 //                    (MultigridPreconditioner.hpp:174-175) as a dense symmetric
 //                    inverse: FP16 packed half tiles (mixed) or the full FP64 matrix.
 //   kUpdateXR, kUpdateR  ConjugateGradient_1.comp + VecDotVec.comp (r.r).
@@ -1366,9 +1366,10 @@ __global__ void __launch_bounds__(256) kGemv64(const double* __restrict__ K, int
 // that maps the largest diagonal entry to 2^14 (|Kinv_ij| <= max diag for an
 // SPD inverse), so every entry above 2^-10 of that maximum keeps FP16's 11-bit
 // significand; the products accumulate in FP32.  The rounding is symmetric, so
-// the coarse operator stays symmetric.  kSymTile reads each tile once and writes
-// its two partial products, K_IJ b_J (for y_I) and K_IJ^T b_I (for y_J,
-// off-diagonal tiles); kSymReduce sums them per row block in a fixed order
+// the coarse operator stays symmetric.  kSymRuns streams runs of consecutive
+// tiles of one row block: it reads each tile once, accumulates K_IJ b_J for
+// y_I over the run and writes K_IJ^T b_I (for y_J, off-diagonal tiles) per
+// tile; kSymRunsReduce sums the partials per row block in a fixed order
 // (deterministic, no atomics) and applies the scale.
 __host__ __device__ inline int64_t symTileCount(int64_t nb) { return nb * (nb + 1) / 2; }
 // Tile index -> (I, J): FP32 square root, corrected exactly in integers (an FP64
@@ -1425,88 +1426,113 @@ __global__ void __launch_bounds__(1024) kMaxDiag(const float* __restrict__ K, in
     }
 }
 
-// One tile per block: 16 x 16 threads, each a 4 x 4 sub-block (four 8-byte
-// row loads).  Row sums reduce over the 16 column groups by shuffles; column
-// sums over the two row groups of a warp by one shuffle, then over the 8
-// warps in shared memory.  part holds 2 x 64 values per tile.
-__global__ void __launch_bounds__(256) kSymTile(const __half* __restrict__ tiles, const float* __restrict__ b,
-                                                float* __restrict__ part, const Scalars* S, int checkDone) {
-    typedef float T;
+// Runs of tiles: row block I's tiles are contiguous in memory; a run is up to
+// SYM_RUN consecutive tiles (I, J0 .. J0 + SYM_RUN - 1) of one row, and one
+// block streams a run.  Runs of row I: ceil((I + 1) / SYM_RUN), numbered in row
+// order from symRunStart(I).
+constexpr int SYM_RUN = 16;
+__host__ __device__ inline int64_t symRunStart(int64_t I) {
+    const int64_t a = I / SYM_RUN, b = I % SYM_RUN;
+    return SYM_RUN * a * (a + 1) / 2 + b * (a + 1);
+}
+
+// One run per block, 16 x 16 threads each holding a 4 x 4 sub-block of every
+// tile (four 8-byte row loads).  The row sums K_IJ b_J accumulate in registers across the
+// run and reduce once (partial of the run at part[run][0..63]); the column sums
+// K_IJ^T b_I of each off-diagonal tile reduce over the row groups through a
+// double-buffered shared array (one barrier per tile) into part[tile][64..127].
+// The next tile's values are loaded while the current one is used.
+__global__ void __launch_bounds__(256) kSymRuns(const __half* __restrict__ tiles, const float* __restrict__ b,
+                                                float* __restrict__ part, int64_t nb, const Scalars* S,
+                                                int checkDone) {
     if (checkDone && S->done) return;
-    __shared__ T colp[8][CT];
-    const int64_t t = blockIdx.x;
-    int64_t I, J;
-    symTileDecode(t, I, J);
+    __shared__ float colp[2][8][CT];
+    const int64_t run = blockIdx.x;
+    int64_t lo = 0, hi = nb - 1;  // largest I with symRunStart(I) <= run
+    while (lo < hi) {
+        const int64_t mid = (lo + hi + 1) / 2;
+        if (symRunStart(mid) <= run) lo = mid;
+        else hi = mid - 1;
+    }
+    const int64_t I = lo;
+    const int64_t J0 = (run - symRunStart(I)) * SYM_RUN, J1 = min(J0 + SYM_RUN, I + 1);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int tc = lane & 15, tr = warp * 2 + (lane >> 4);
-    const __half* K = tiles + t * (CT * CT);
-    // Products in packed FP32x2: a row sum keeps its even and odd columns in
-    // the two halves of one register pair, a column pair shares one pair.
-    const float2 bJ01 = make_float2(b[J * CT + 4 * tc], b[J * CT + 4 * tc + 1]);
-    const float2 bJ23 = make_float2(b[J * CT + 4 * tc + 2], b[J * CT + 4 * tc + 3]);
-    T bI[4], rs[4], cs[4];
+    const int64_t rowTile = I * (I + 1) / 2;
+    float bI[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) bI[j] = b[I * CT + 4 * tr + j];
-    float2 cs01 = make_float2(0.f, 0.f), cs23 = make_float2(0.f, 0.f);
+    float rs[4] = {0.f, 0.f, 0.f, 0.f};
+    uint2 nxt[4];
+    auto loadTile = [&](int64_t J, uint2 (&raw)[4]) {
+        const __half* K = tiles + (rowTile + J) * (CT * CT);
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        const uint2 raw = *reinterpret_cast<const uint2*>(K + (4 * tr + i) * CT + 4 * tc);
-        const float2 k01 = __half22float2(*reinterpret_cast<const __half2*>(&raw.x));
-        const float2 k23 = __half22float2(*reinterpret_cast<const __half2*>(&raw.y));
-        const float2 r2 = __ffma2_rn(k23, bJ23, __fmul2_rn(k01, bJ01));
-        rs[i] = r2.x + r2.y;
-        const float2 bi = make_float2(bI[i], bI[i]);
-        cs01 = __ffma2_rn(k01, bi, cs01);
-        cs23 = __ffma2_rn(k23, bi, cs23);
+        for (int i = 0; i < 4; ++i) raw[i] = *reinterpret_cast<const uint2*>(K + (4 * tr + i) * CT + 4 * tc);
+    };
+    loadTile(J0, nxt);
+    int buf = 0;
+    for (int64_t J = J0; J < J1; ++J) {
+        uint2 cur[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) cur[i] = nxt[i];
+        if (J + 1 < J1) loadTile(J + 1, nxt);
+        const float2 bJ01 = make_float2(b[J * CT + 4 * tc], b[J * CT + 4 * tc + 1]);
+        const float2 bJ23 = make_float2(b[J * CT + 4 * tc + 2], b[J * CT + 4 * tc + 3]);
+        float2 cs01 = make_float2(0.f, 0.f), cs23 = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const float2 k01 = __half22float2(*reinterpret_cast<const __half2*>(&cur[i].x));
+            const float2 k23 = __half22float2(*reinterpret_cast<const __half2*>(&cur[i].y));
+            const float2 r2 = __ffma2_rn(k23, bJ23, __fmul2_rn(k01, bJ01));
+            rs[i] += r2.x + r2.y;
+            const float2 bi = make_float2(bI[i], bI[i]);
+            cs01 = __ffma2_rn(k01, bi, cs01);
+            cs23 = __ffma2_rn(k23, bi, cs23);
+        }
+        if (J != I) {  // the same for the whole block
+            float cs[4] = {cs01.x, cs01.y, cs23.x, cs23.y};
+#pragma unroll
+            for (int j = 0; j < 4; ++j) cs[j] += __shfl_xor_sync(0xffffffffu, cs[j], 16);
+            if (lane < 16) {
+#pragma unroll
+                for (int j = 0; j < 4; ++j) colp[buf][warp][4 * tc + j] = cs[j];
+            }
+            __syncthreads();
+            if (threadIdx.x < CT) {
+                float sum = 0.f;
+#pragma unroll
+                for (int w = 0; w < 8; ++w) sum += colp[buf][w][threadIdx.x];
+                part[(rowTile + J) * (2 * CT) + CT + threadIdx.x] = sum;
+            }
+            buf ^= 1;
+        }
     }
-    cs[0] = cs01.x;
-    cs[1] = cs01.y;
-    cs[2] = cs23.x;
-    cs[3] = cs23.y;
 #pragma unroll
     for (int o = 1; o < 16; o <<= 1)
 #pragma unroll
         for (int i = 0; i < 4; ++i) rs[i] += __shfl_xor_sync(0xffffffffu, rs[i], o);
-    T* pt = part + t * (2 * CT);
     if (tc == 0) {
 #pragma unroll
-        for (int i = 0; i < 4; ++i) pt[4 * tr + i] = rs[i];
-    }
-    const bool offDiag = I != J;
-    if (offDiag) {
-#pragma unroll
-        for (int j = 0; j < 4; ++j) cs[j] += __shfl_xor_sync(0xffffffffu, cs[j], 16);
-        if (lane < 16) {
-#pragma unroll
-            for (int j = 0; j < 4; ++j) colp[warp][4 * tc + j] = cs[j];
-        }
-    }
-    __syncthreads();
-    if (offDiag && threadIdx.x < CT) {
-        T s = T(0);
-#pragma unroll
-        for (int w = 0; w < 8; ++w) s += colp[w][threadIdx.x];
-        pt[CT + threadIdx.x] = s;
+        for (int i = 0; i < 4; ++i) part[run * (2 * CT) + 4 * tr + i] = rs[i];
     }
 }
 
-// y_I = scale (sum_{J <= I} (K_IJ b_J) + sum_{I' > I} (K_I'I^T b_I')); 16 groups
-// of 64 threads split the tiles of row block I, then one group adds the 16 sums.
-__global__ void __launch_bounds__(1024) kSymReduce(const float* __restrict__ part, int64_t nb, int64_t n,
-                                                   const int32_t* __restrict__ freeDof, float scale,
-                                                   float* __restrict__ zc, const Scalars* S, int checkDone) {
-    typedef float T;
+// y_I = scale (sum over the runs of row I of their row partials + sum_{I' > I}
+// (K_I'I^T b_I')), in a fixed order.
+__global__ void __launch_bounds__(1024) kSymRunsReduce(const float* __restrict__ part, int64_t nb, int64_t n,
+                                                       const int32_t* __restrict__ freeDof, float scale,
+                                                       float* __restrict__ zc, const Scalars* S, int checkDone) {
     if (checkDone && S->done) return;
-    __shared__ T red[16][CT];
+    __shared__ float red[16][CT];
     const int64_t I = blockIdx.x;
     const int r = threadIdx.x & (CT - 1), grp = threadIdx.x >> 6;
-    T s = T(0);
-    for (int64_t J = grp; J <= I; J += 16) s += part[(I * (I + 1) / 2 + J) * (2 * CT) + r];
+    float s = 0.f;
+    for (int64_t q = symRunStart(I) + grp; q < symRunStart(I + 1); q += 16) s += part[q * (2 * CT) + r];
     for (int64_t Ip = I + 1 + grp; Ip < nb; Ip += 16) s += part[(Ip * (Ip + 1) / 2 + I) * (2 * CT) + CT + r];
     red[grp][r] = s;
     __syncthreads();
     if (grp == 0) {
-        T y = T(0);
+        float y = 0.f;
 #pragma unroll
         for (int q = 0; q < 16; ++q) y += red[q][r];
         const int64_t i = I * CT + r;
@@ -1982,8 +2008,8 @@ int launchCoarseSolve(const LaunchCtx& c, CoarseInv<T> Kinv, int64_t n, const in
         return 2;
     } else {
         const int64_t nb = coarseBlocks(n);
-        kSymTile<<<(unsigned)symTileCount(nb), 256, 0, c.stream>>>(Kinv.K, tmp, part, c.S, checkDone);
-        kSymReduce<<<(unsigned)nb, 1024, 0, c.stream>>>(part, nb, n, freeDof, Kinv.scale, zc, c.S, checkDone);
+        kSymRuns<<<(unsigned)symRunStart(nb), 256, 0, c.stream>>>(Kinv.K, tmp, part, nb, c.S, checkDone);
+        kSymRunsReduce<<<(unsigned)nb, 1024, 0, c.stream>>>(part, nb, n, freeDof, Kinv.scale, zc, c.S, checkDone);
         return 3;
     }
 }
