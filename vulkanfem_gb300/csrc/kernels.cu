@@ -2161,6 +2161,8 @@ int launchInitScalars(cudaStream_t s, Scalars* S, double tol, long long maxIter,
 // until the process exits.  All calls share it, so calls that overlap on the GPU
 // race; each call clears the ticket and scalars before its kernel.
 namespace {
+// Partials of the product's grid reduction, which carries two sums per block
+// (x.(Kx) and the unused second dot).
 constexpr size_t kNoAllocPartialBytes = 2 * (size_t)kMaxRedBlocks * sizeof(double);
 constexpr size_t kNoAllocBytes = kNoAllocPartialBytes + 1024;
 static_assert(sizeof(Scalars) + 256 <= 1024, "scalar block does not fit the no-allocation scratch");
